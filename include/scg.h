@@ -1,0 +1,193 @@
+/*
+ * solvcon-gb300 C ABI: the drop-in boundary of the GPU CESE march.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, integer status codes.
+ * Every function returns SCG_OK (0) or one of the SCG_E* codes below, and the
+ * message of the most recent failure on the calling thread is returned by
+ * scg_last_error().  No C++ exception crosses this boundary.  Arrays are
+ * exchanged in the reference's own layout: one contiguous row-major FP64 (or
+ * int32) table per array, ghost rows first, so row i of a table with nghost
+ * ghost rows is stored at (i + nghost) * row_width.
+ *
+ * Each declaration names the reference interface it replaces, by file:line
+ * within solvcon's source tree.  A handle is not thread-safe: use one handle
+ * from one thread at a time.
+ */
+
+#ifndef SCG_H
+#define SCG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (map onto the reference's exception types). */
+#define SCG_OK 0
+#define SCG_EINVAL 1   /* std::invalid_argument -> ValueError */
+#define SCG_ERANGE 2   /* std::out_of_range -> IndexError */
+#define SCG_ERUNTIME 3 /* std::runtime_error -> RuntimeError */
+#define SCG_ECUDA 4    /* CUDA runtime failure -> RuntimeError */
+#define SCG_ENOMEM 5   /* allocation failure -> MemoryError */
+
+typedef struct scg_mesh scg_mesh;
+typedef struct scg_euler scg_euler;
+typedef struct scg_e1d scg_e1d;
+typedef struct scg_st scg_st;
+
+/* Message of the last failure on this thread ("" if none). */
+const char * scg_last_error(void);
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t scg_launch_count(void);
+/* Library version string. */
+const char * scg_version(void);
+
+/* ------------------------------------------------------------------------
+ * Unstructured mesh, host side.
+ * Replaces solvcon::StaticMesh (cpp/solvcon/mesh/StaticMesh.hpp:264-456) as
+ * bound to Python by cpp/solvcon/mesh/pymod/wrap_StaticMesh.cpp:61-181.
+ * ---------------------------------------------------------------------- */
+
+/* Mesh array ids for scg_mesh_array. */
+#define SCG_MESH_NDCRD 0
+#define SCG_MESH_FCCND 1
+#define SCG_MESH_FCNML 2
+#define SCG_MESH_FCARA 3
+#define SCG_MESH_CLCND 4
+#define SCG_MESH_CLVOL 5
+#define SCG_MESH_FCTPN 6
+#define SCG_MESH_CLTPN 7
+#define SCG_MESH_CLGRP 8
+#define SCG_MESH_FCNDS 9
+#define SCG_MESH_FCCLS 10
+#define SCG_MESH_CLNDS 11
+#define SCG_MESH_CLFCS 12
+#define SCG_MESH_EDNDS 13
+#define SCG_MESH_BNDFCS 14
+
+/* StaticMesh(ndim, nnode, nface, ncell): StaticMesh.hpp:290-311. */
+int scg_mesh_create(int ndim, int64_t nnode, int64_t nface, int64_t ncell, scg_mesh ** out);
+int scg_mesh_destroy(scg_mesh * mesh);
+/* out[10] = ndim nnode nface ncell nbound ngstnode ngstface ngstcell nedge nbcs
+ * (wrap_StaticMesh.cpp:97-106). */
+int scg_mesh_sizes(const scg_mesh * mesh, int64_t * out);
+/* Pointer to the live host table of one mesh array (valid until the next
+ * build call); *dtype is 0 for float64 and 1 for int32; shape has up to 2
+ * extents and nghost is the first-axis ghost count (StaticMesh.hpp:434-451). */
+int scg_mesh_array(scg_mesh * mesh, int which, void ** data, int64_t * shape, int * nd, int64_t * nghost,
+                   int * dtype);
+/* build_interior(do_metric, do_edge): StaticMesh.hpp:363-374. */
+int scg_mesh_build_interior(scg_mesh * mesh, int do_metric, int do_edge);
+/* build_edge: StaticMesh_interior.cpp:545. */
+int scg_mesh_build_edge(scg_mesh * mesh);
+/* add_bc(name, faces): StaticMesh_boundary.cpp:68-78. */
+int scg_mesh_add_bc(scg_mesh * mesh, const char * name, const int32_t * faces, int64_t nface);
+/* Name and facn table [nbound][3] of boundary group ibc (StaticMesh.hpp:159-251);
+ * name is copied into buf of length buflen; facn may be null to query nbound. */
+int scg_mesh_bc(const scg_mesh * mesh, int64_t ibc, char * buf, int64_t buflen, int32_t * facn, int64_t * nbound);
+/* build_boundary: StaticMesh_boundary.cpp:103-182. */
+int scg_mesh_build_boundary(scg_mesh * mesh);
+/* build_ghost: StaticMesh_boundary.cpp:185-240. */
+int scg_mesh_build_ghost(scg_mesh * mesh);
+
+/* ------------------------------------------------------------------------
+ * Multi-dimensional Euler CESE core on the GPU.
+ * Replaces solvcon::EulerCore (cpp/solvcon/multidim/euler.hpp:56-211) as bound
+ * by cpp/solvcon/multidim/pymod/wrap_multidim.cpp:184-414.
+ * ---------------------------------------------------------------------- */
+
+/* Precision of the march. */
+#define SCG_FP64 0        /* the reference's FP64 arithmetic */
+#define SCG_FP32_GEOM64 1 /* FP32 state and flux, FP64 geometry tables */
+#define SCG_FP32 2        /* FP32 state, flux and stored geometry (computed FP64) */
+
+/* EulerCore array ids (wrap_multidim.cpp:381-408). */
+#define SCG_EA_CEVOL 0
+#define SCG_EA_CECND 1
+#define SCG_EA_SFCND 2
+#define SCG_EA_SFNML 3
+#define SCG_EA_SO0C 4
+#define SCG_EA_SO0N 5
+#define SCG_EA_SO0T 6
+#define SCG_EA_SO1C 7
+#define SCG_EA_SO1N 8
+#define SCG_EA_STM 9
+#define SCG_EA_CFLO 10
+#define SCG_EA_CFLC 11
+#define SCG_EA_GAMMA 12
+
+/* EulerCore operation ids for scg_euler_op (wrap_multidim.cpp:269-319). */
+#define SCG_OP_PREPARE_CE 0
+#define SCG_OP_UPDATE 1
+#define SCG_OP_CALC_SOLT 2
+#define SCG_OP_CALC_SOLN 3
+#define SCG_OP_BC_SOLN 4
+#define SCG_OP_CALC_CFL 5
+#define SCG_OP_CALC_DSOLN 6
+#define SCG_OP_BC_DSOLN 7
+#define SCG_OP_MARCH_SUBSTEP 8
+
+/* Boundary kinds (euler.hpp:26-31). */
+#define SCG_BC_NONREFL 0
+#define SCG_BC_SLIPWALL 1
+#define SCG_BC_INLET 2
+
+/* Parameter ids. */
+#define SCG_PARAM_SIGMA0 0
+#define SCG_PARAM_TAUMIN 1
+#define SCG_PARAM_TAUSCALE 2
+#define SCG_PARAM_TIME_INCREMENT 3 /* read-only */
+
+/* EulerCore(mesh, time_increment): euler_ce.cpp:15-29 (builds CE geometry on
+ * the device).  The mesh must have its ghost layer built; the core copies what
+ * it needs, so the mesh may be destroyed afterwards. */
+int scg_euler_create(const scg_mesh * mesh, double time_increment, int precision, scg_euler ** out);
+int scg_euler_destroy(scg_euler * core);
+/* out[5] = ndim ncell ngstcell neq precision (wrap_multidim.cpp:227-231). */
+int scg_euler_info(const scg_euler * core, int64_t * out);
+/* sigma0/taumin/tauscale properties and time_increment (wrap_multidim.cpp:311-316). */
+int scg_euler_get_param(const scg_euler * core, int which, double * value);
+int scg_euler_set_param(scg_euler * core, int which, double value);
+/* Shape (up to 3 extents) and ghost count of an array in the reference layout. */
+int scg_euler_array_shape(const scg_euler * core, int which, int64_t * shape, int * nd, int64_t * nghost);
+/* Copy a whole array (ghost rows first) device -> host / host -> device;
+ * count is the number of float64 elements in the host buffer. */
+int scg_euler_get(scg_euler * core, int which, double * host, int64_t count);
+int scg_euler_set(scg_euler * core, int which, const double * host, int64_t count);
+/* init_solution(gamma, rho, v, p): euler_solution.cpp:188-233. */
+int scg_euler_init_solution(scg_euler * core, double gamma, double rho, const double * v, int nv, double p);
+/* add_nonrefl/add_slipwall/add_inlet: euler_bc.cpp:324-391. */
+int scg_euler_add_bc(scg_euler * core, int kind, const int32_t * faces, int64_t nface, const double * value,
+                     int64_t nvalue);
+/* clear_bc: euler.hpp:152. */
+int scg_euler_clear_bc(scg_euler * core);
+/* get_normal_matrix(ifc) -> out[ndim*ndim]: euler_bc.cpp:393-425. */
+int scg_euler_normal_matrix(const scg_euler * core, int32_t ifc, double * out);
+/* prepare_ce, update, calc_solt, calc_soln, bc_soln, calc_cfl, calc_dsoln,
+ * bc_dsoln, march_substep: euler_march.cpp:307-348 and friends.  Synchronous. */
+int scg_euler_op(scg_euler * core, int op);
+/* march(steps): euler_march.cpp:350-359.  Asynchronous on the core's stream;
+ * scg_euler_sync waits for it. */
+int scg_euler_march(scg_euler * core, int64_t steps);
+int scg_euler_sync(scg_euler * core);
+/* Run the core on a caller-owned cudaStream_t (null restores its own). */
+int scg_euler_set_stream(scg_euler * core, void * cuda_stream);
+/* W-3/4 limiter firing bits of the last calc_dsoln per body cell: bit i set
+ * when sigma_max of equation i was capped below sigma0/|cfl|
+ * (euler_gradient.cpp:102-108).  out has ncell bytes. */
+int scg_euler_limiter_mask(scg_euler * core, uint8_t * out);
+/* FP64 totals sum_i so0n[i, :] * clvol[i] over body cells (out[neq]); the
+ * mass/momentum/energy integrals of solvcon's EulerField
+ * (solvcon/multidim/euler/_field.py:16-148). */
+int scg_euler_totals(scg_euler * core, double * out);
+/* min and max of cflo over body cells (EulerField.calc_cfl_range). */
+int scg_euler_cfl_range(scg_euler * core, double * out);
+/* Device memory held by the core, in bytes. */
+int scg_euler_device_bytes(const scg_euler * core, int64_t * out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCG_H */

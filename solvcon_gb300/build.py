@@ -1,0 +1,85 @@
+"""Build recipe of the native library (libscg.so) for sm_103a.
+
+Compiles every translation unit under csrc/ with nvcc in parallel and links
+them into solvcon_gb300/_lib/libscg.so, in-tree.  Host C++ is compiled with
+-ffp-contract=off so that the host mesh builder produces the same bits on the
+x86 build host and on the Arm GPU host.
+"""
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUTDIR = os.path.join(HERE, "_lib")
+OBJDIR = os.path.join(HERE, "_build")
+LIBNAME = "libscg.so"
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"),
+                        "bin", "nvcc")
+    return cand if os.path.exists(cand) else (shutil.which("nvcc") or cand)
+
+
+def sources():
+    out = []
+    for name in sorted(os.listdir(CSRC)):
+        if name.endswith((".cu", ".cpp")):
+            out.append(os.path.join(CSRC, name))
+    return out
+
+
+def headers():
+    hs = [os.path.join(CSRC, n) for n in os.listdir(CSRC)
+          if n.endswith((".hpp", ".cuh", ".h"))]
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    if os.path.isdir(inc):
+        hs += [os.path.join(inc, n) for n in os.listdir(inc)]
+    return hs
+
+
+def _compile(src, extra):
+    obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+    hmax = max([os.path.getmtime(h) for h in headers()] + [0])
+    if os.path.exists(obj) and \
+            os.path.getmtime(obj) >= max(os.path.getmtime(src), hmax):
+        return obj
+    cmd = [nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++17",
+           "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+           "--expt-relaxed-constexpr", "-I" + CSRC, "-c", src, "-o", obj]
+    cmd += extra
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("nvcc failed on %s:\n%s\n%s" %
+                           (src, " ".join(cmd), res.stderr[-8000:]))
+    return obj
+
+
+def build(verbose=False, extra=()):
+    """Compile and link libscg.so; returns its path."""
+    os.makedirs(OUTDIR, exist_ok=True)
+    os.makedirs(OBJDIR, exist_ok=True)
+    srcs = sources()
+    with concurrent.futures.ThreadPoolExecutor(
+            max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+    lib = os.path.join(OUTDIR, LIBNAME)
+    if not os.path.exists(lib) or \
+            os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc(), ARCH, "-shared", "-o", lib] + objs + ["-lcudart"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" %
+                               (" ".join(cmd), res.stderr[-8000:]))
+    if verbose:
+        print("built", lib)
+    return lib
+
+
+if __name__ == "__main__":
+    build(verbose=True, extra=sys.argv[1:])

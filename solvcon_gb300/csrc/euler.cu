@@ -1,0 +1,1162 @@
+/*
+ * GPU Euler core: device state, the per-operation kernels of the EulerCore
+ * surface, and the fused march.
+ *
+ * Logical arrays of the reference and where they live here (cur/nxt are the
+ * two record buffers, swapped by update() just as the reference swaps so0c
+ * with so0n and so1c with so1n, euler.hpp:123-127):
+ *   so0c = cur.so0, so1c = cur.so1, so0n = nxt.so0, so1n = nxt.so1,
+ *   so0t = rec[tbuf].so0t   (so0t is not swapped by update()).
+ * The fused march additionally leaves nxt.so0t holding calc_solt of the new
+ * state, so the next substep skips its calc_solt pass (see march_substep()).
+ */
+
+#include "euler_core.hpp"
+#include "euler_kernels.cuh"
+#include "euler_setup.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace scg
+{
+
+using namespace dev;
+
+namespace
+{
+
+constexpr int BLOCK = 128;
+
+inline unsigned grid_for(int64_t n)
+{
+    return static_cast<unsigned>((n + BLOCK - 1) / BLOCK);
+}
+
+// --------------------------------------------------------------------------
+// Per-operation kernels (one thread per row or body cell).
+
+template <int ND, typename R>
+__global__ void k_solt_rows(R * rec, R const * gamma, int64_t nrow)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrow)
+    {
+        return;
+    }
+    R v[2 * NEQ + NEQ * ND];
+    load_rec<ND, R>(rec + r * Dim<ND>::RS, v);
+    R t[NEQ];
+    solt_row<ND, R>(v, v + 2 * NEQ, gamma[r], t);
+    for (int i = 0; i < NEQ; ++i)
+    {
+        rec[r * Dim<ND>::RS + NEQ + i] = t[i];
+    }
+}
+
+template <int ND, typename R>
+__global__ void k_copy_field(R const * src, R * dst, int64_t nrow, int off, int width)
+{
+    int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrow)
+    {
+        return;
+    }
+    for (int k = 0; k < width; ++k)
+    {
+        dst[r * Dim<ND>::RS + off + k] = src[r * Dim<ND>::RS + off + k];
+    }
+}
+
+template <int ND, typename R, typename G>
+__global__ void k_soln(MarchArgs<R, G> a)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (icl >= a.ncell)
+    {
+        return;
+    }
+    R so0n[NEQ];
+    int const ct = a.ctype[icl];
+    if constexpr (ND == 2)
+    {
+        if (ct == 4)
+            soln_cell<4, R, G, false>(a, icl, so0n, nullptr, nullptr);
+        else
+            soln_cell<3, R, G, false>(a, icl, so0n, nullptr, nullptr);
+    }
+    else
+    {
+        switch (ct)
+        {
+        case 6: soln_cell<6, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
+        case 5: soln_cell<5, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
+        case 7: soln_cell<7, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
+        default: soln_cell<8, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
+        }
+    }
+    R * out = a.nxt + (icl + a.ngst) * Dim<ND>::RS;
+    for (int i = 0; i < NEQ; ++i)
+    {
+        out[i] = so0n[i];
+    }
+}
+
+template <int ND, typename R, typename G>
+__global__ void k_cfl(MarchArgs<R, G> a)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (icl >= a.ncell)
+    {
+        return;
+    }
+    int64_t const row = icl + a.ngst;
+    R * out = a.nxt + row * Dim<ND>::RS;
+    R s[NEQ];
+    for (int i = 0; i < NEQ; ++i)
+    {
+        s[i] = out[i];
+    }
+    cfl_cell<ND, R, G>(a, icl, row, s);
+    out[NEQ - 1] = s[NEQ - 1];
+}
+
+template <int ND, typename R, typename G>
+__global__ void k_dsoln(MarchArgs<R, G> a)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (icl >= a.ncell)
+    {
+        return;
+    }
+    int64_t const row = icl + a.ngst;
+    R * out = a.nxt + row * Dim<ND>::RS;
+    R s[NEQ];
+    for (int i = 0; i < NEQ; ++i)
+    {
+        s[i] = out[i];
+    }
+    R const cflc = a.cflc[row];
+    R g[NEQ * ND];
+    int const ct = a.ctype[icl];
+    if constexpr (ND == 2)
+    {
+        if (ct == 4)
+            dsoln_cell<4, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g);
+        else
+            dsoln_cell<3, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g);
+    }
+    else
+    {
+        switch (ct)
+        {
+        case 6: dsoln_cell<6, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
+        case 5: dsoln_cell<5, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
+        case 7: dsoln_cell<7, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
+        default: dsoln_cell<8, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
+        }
+    }
+    for (int i = 0; i < NEQ * ND; ++i)
+    {
+        out[2 * NEQ + i] = g[i];
+    }
+}
+
+// bc_soln over every ghost row with a registered condition.
+template <int ND, typename R, typename G>
+__global__ void k_bc0(MarchArgs<R, G> a, int32_t const * gint)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= a.ngst || a.gkind[g] < 0)
+    {
+        return;
+    }
+    R const * in = a.nxt + static_cast<int64_t>(gint[g]) * Dim<ND>::RS;
+    R s[NEQ], o[NEQ];
+    for (int i = 0; i < NEQ; ++i)
+    {
+        s[i] = in[i];
+    }
+    bc0_ghost<ND, R>(a.gkind[g], a.gnml + g * ND, a.gval + g * NEQ, s, o);
+    R * out = a.nxt + g * Dim<ND>::RS;
+    for (int i = 0; i < NEQ; ++i)
+    {
+        out[i] = o[i];
+    }
+}
+
+// bc_dsoln over every ghost row with a registered condition.
+template <int ND, typename R, typename G>
+__global__ void k_bc1(MarchArgs<R, G> a, int32_t const * gint)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= a.ngst || a.gkind[g] < 0)
+    {
+        return;
+    }
+    R const * in = a.cur + static_cast<int64_t>(gint[g]) * Dim<ND>::RS + 2 * NEQ;
+    R s[NEQ * ND], o[NEQ * ND];
+    for (int i = 0; i < NEQ * ND; ++i)
+    {
+        s[i] = in[i];
+    }
+    bc1_ghost<ND, R>(a.gkind[g], a.gnml + g * ND, s, o);
+    R * out = a.nxt + g * Dim<ND>::RS + 2 * NEQ;
+    for (int i = 0; i < NEQ * ND; ++i)
+    {
+        out[i] = o[i];
+    }
+}
+
+// init_solution (euler_solution.cpp:188-233): so0n body rows and every gamma.
+template <int ND, typename R>
+__global__ void k_init(R * nxt, R * gamma, int64_t ngst, int64_t nrow, double ga, double rho, double m0, double m1,
+                       double m2, double energy)
+{
+    constexpr int NEQ = ND + 2;
+    int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrow)
+    {
+        return;
+    }
+    gamma[r] = R(ga);
+    if (r >= ngst)
+    {
+        R * o = nxt + r * Dim<ND>::RS;
+        o[0] = R(rho);
+        o[1] = R(m0);
+        o[2] = R(m1);
+        if constexpr (ND == 3)
+        {
+            o[3] = R(m2);
+        }
+        o[NEQ - 1] = R(energy);
+    }
+}
+
+// Record field <-> FP64 reference-layout table.
+template <int ND, typename R>
+__global__ void k_get_field(R const * rec, double * out, int64_t nrow, int off, int width)
+{
+    int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrow)
+    {
+        return;
+    }
+    for (int k = 0; k < width; ++k)
+    {
+        out[r * width + k] = double(rec[r * Dim<ND>::RS + off + k]);
+    }
+}
+
+template <int ND, typename R>
+__global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, int width)
+{
+    int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= nrow)
+    {
+        return;
+    }
+    for (int k = 0; k < width; ++k)
+    {
+        rec[r * Dim<ND>::RS + off + k] = R(in[r * width + k]);
+    }
+}
+
+template <typename R>
+__global__ void k_to_f64(R const * in, double * out, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        out[i] = double(in[i]);
+    }
+}
+
+template <typename R>
+__global__ void k_from_f64(double const * in, R * out, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        out[i] = R(in[i]);
+    }
+}
+
+// Per-block FP64 partial sums of so0n[:, i] * clvol (Kahan inside a thread,
+// tree across the block), and min/max of cflo.
+template <int ND, typename R>
+__global__ void k_totals(R const * nxt, double const * clvol, R const * cflo, int64_t ngst, int64_t ncell,
+                         double * part)
+{
+    constexpr int NEQ = ND + 2;
+    __shared__ double sh[NEQ + 2][BLOCK];
+    double s[NEQ], c[NEQ];
+    for (int i = 0; i < NEQ; ++i)
+    {
+        s[i] = 0.0;
+        c[i] = 0.0;
+    }
+    double lo = 1.79769313486231570815e+308, hi = -1.79769313486231570815e+308;
+    for (int64_t icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; icl < ncell;
+         icl += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        int64_t const row = icl + ngst;
+        double const v = clvol[row];
+        for (int i = 0; i < NEQ; ++i)
+        {
+            double const y = double(nxt[row * Dim<ND>::RS + i]) * v - c[i];
+            double const t = s[i] + y;
+            c[i] = (t - s[i]) - y;
+            s[i] = t;
+        }
+        double const cf = double(cflo[row]);
+        lo = fmin(lo, cf);
+        hi = fmax(hi, cf);
+    }
+    for (int i = 0; i < NEQ; ++i)
+    {
+        sh[i][threadIdx.x] = s[i];
+    }
+    sh[NEQ][threadIdx.x] = lo;
+    sh[NEQ + 1][threadIdx.x] = hi;
+    __syncthreads();
+    for (int w = BLOCK / 2; w > 0; w >>= 1)
+    {
+        if (threadIdx.x < w)
+        {
+            for (int i = 0; i < NEQ; ++i)
+            {
+                sh[i][threadIdx.x] += sh[i][threadIdx.x + w];
+            }
+            sh[NEQ][threadIdx.x] = fmin(sh[NEQ][threadIdx.x], sh[NEQ][threadIdx.x + w]);
+            sh[NEQ + 1][threadIdx.x] = fmax(sh[NEQ + 1][threadIdx.x], sh[NEQ + 1][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        for (int i = 0; i < NEQ + 2; ++i)
+        {
+            part[blockIdx.x * (NEQ + 2) + i] = sh[i][0];
+        }
+    }
+}
+
+} // namespace
+
+// --------------------------------------------------------------------------
+// Base-class helpers.
+
+void EulerCoreBase::array_shape(int which, int64_t * shape, int * nd, int64_t * nghost) const
+{
+    int64_t const tot = ngstcell + ncell;
+    *nghost = ngstcell;
+    switch (which)
+    {
+    case EA_CEVOL: shape[0] = tot; shape[1] = 7; *nd = 2; break;
+    case EA_CECND: shape[0] = tot; shape[1] = 7 * ndim; *nd = 2; break;
+    case EA_SFCND:
+    case EA_SFNML:
+        shape[0] = ncell; shape[1] = 24; shape[2] = ndim; *nd = 3; *nghost = 0; break;
+    case EA_SO0C:
+    case EA_SO0N:
+    case EA_SO0T:
+    case EA_STM: shape[0] = tot; shape[1] = neq; *nd = 2; break;
+    case EA_SO1C:
+    case EA_SO1N: shape[0] = tot; shape[1] = neq; shape[2] = ndim; *nd = 3; break;
+    case EA_CFLO:
+    case EA_CFLC:
+    case EA_GAMMA: shape[0] = tot; *nd = 1; break;
+    default: throw std::invalid_argument("EulerCore: unknown array id " + std::to_string(which));
+    }
+}
+
+int64_t EulerCoreBase::array_size(int which) const
+{
+    int64_t shape[3] = {1, 1, 1};
+    int nd = 0;
+    int64_t ng = 0;
+    array_shape(which, shape, &nd, &ng);
+    int64_t n = 1;
+    for (int k = 0; k < nd; ++k)
+    {
+        n *= shape[k];
+    }
+    return n;
+}
+
+// add_bc with the reference's validation (euler_bc.cpp:324-391).
+void EulerCoreBase::add_bc(int kind, std::vector<int32_t> const & faces, std::vector<double> const & value)
+{
+    if (kind < BC_NONREFL || kind > BC_INLET)
+    {
+        throw std::invalid_argument("EulerCore::add_bc: unknown boundary kind " + std::to_string(kind));
+    }
+    for (int32_t const ifc : faces)
+    {
+        if (ifc < 0 || ifc >= m_nface)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: face " + std::to_string(ifc) + " out of range [0, " +
+                                        std::to_string(m_nface) + ")");
+        }
+        if (m_fccls[static_cast<size_t>((ifc + m_ngstface) * 4 + 1)] >= 0)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: face " + std::to_string(ifc) + " is not a boundary face");
+        }
+    }
+    if (kind == BC_INLET)
+    {
+        size_t const expect = static_cast<size_t>(ndim) + 3;
+        if (value.size() != expect)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: inlet value size " + std::to_string(value.size()) +
+                                        " must equal ndim+3 = " + std::to_string(expect));
+        }
+        double const rho = value[0];
+        double const p = value[1 + ndim];
+        double const ga = value[2 + ndim];
+        if (ga <= 1.0)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: inlet gamma " + std::to_string(ga) + " must be > 1");
+        }
+        if (rho <= 0.0)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: inlet rho " + std::to_string(rho) + " must be > 0");
+        }
+        if (p < 0.0)
+        {
+            throw std::invalid_argument("EulerCore::add_bc: inlet pressure " + std::to_string(p) + " must be >= 0");
+        }
+    }
+    m_bcs.push_back(EulerBoundary{kind, faces, value});
+    m_bc_dirty = true;
+}
+
+void EulerCoreBase::clear_bc()
+{
+    m_bcs.clear();
+    m_bc_dirty = true;
+}
+
+// normal_matrix (euler_bc.cpp:87-128): rows are the outward unit normal and a
+// tangent basis.
+void EulerCoreBase::normal_matrix(int32_t ifc, double * out) const
+{
+    if (ifc < 0 || ifc >= m_nface)
+    {
+        throw std::out_of_range("EulerCore: face " + std::to_string(ifc) + " out of range [0, " +
+                                std::to_string(m_nface) + ")");
+    }
+    double const * n = &m_fcnml[static_cast<size_t>((ifc + m_ngstface) * ndim)];
+    if (ndim == 2)
+    {
+        out[0] = n[0];
+        out[1] = n[1];
+        out[2] = -n[1];
+        out[3] = n[0];
+        return;
+    }
+    double axis[3] = {0.0, 0.0, 0.0};
+    double const ax = std::fabs(n[0]), ay = std::fabs(n[1]), az = std::fabs(n[2]);
+    if (ax <= ay && ax <= az)
+        axis[0] = 1.0;
+    else if (ay <= az)
+        axis[1] = 1.0;
+    else
+        axis[2] = 1.0;
+    double t1[3] = {n[1] * axis[2] - n[2] * axis[1], n[2] * axis[0] - n[0] * axis[2], n[0] * axis[1] - n[1] * axis[0]};
+    double const len = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (double & v : t1)
+    {
+        v /= len;
+    }
+    double const t2[3] = {n[1] * t1[2] - n[2] * t1[1], n[2] * t1[0] - n[0] * t1[2], n[0] * t1[1] - n[1] * t1[0]};
+    for (int d = 0; d < 3; ++d)
+    {
+        out[d] = n[d];
+        out[3 + d] = t1[d];
+        out[6 + d] = t2[d];
+    }
+}
+
+// --------------------------------------------------------------------------
+// Templated implementation.
+
+namespace
+{
+
+template <int ND, typename R, typename G>
+class EulerCoreImpl : public EulerCoreBase
+{
+public:
+    static constexpr int NEQ = ND + 2;
+    static constexpr int RS = Dim<ND>::RS;
+    static constexpr int KF = Dim<ND>::KF;
+
+    EulerCoreImpl(HostMesh const & mesh, double dt, int prec)
+    {
+        ndim = ND;
+        neq = NEQ;
+        ncell = mesh.ncell;
+        ngstcell = mesh.ngstcell;
+        time_increment = dt;
+        precision = prec;
+        nrow = ncell + ngstcell;
+        m_nface = mesh.nface;
+        m_ngstface = mesh.ngstface;
+        m_fccls = mesh.fccls.buf;
+        m_fcnml = mesh.fcnml.buf;
+        m_stm.assign(static_cast<size_t>(nrow * NEQ), 0.0);
+        cuda_check(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        stream = own_stream;
+
+        // Mesh tables on the device.
+        up(d_ndcrd, mesh.ndcrd.buf);
+        up(d_fccnd, mesh.fccnd.buf);
+        up(d_clcnd, mesh.clcnd.buf);
+        up(d_fcnds, mesh.fcnds.buf);
+        up(d_fccls, mesh.fccls.buf);
+        up(d_clfcs, mesh.clfcs.buf);
+        up(d_cltpn, mesh.cltpn.buf);
+        up(d_clvol, mesh.clvol.buf);
+        mv.ndim = ND;
+        mv.ncell = ncell;
+        mv.ngstcell = ngstcell;
+        mv.ngstface = mesh.ngstface;
+        mv.ngstnode = mesh.ngstnode;
+        mv.ndcrd = d_ndcrd.ptr;
+        mv.fccnd = d_fccnd.ptr;
+        mv.clcnd = d_clcnd.ptr;
+        mv.fcnds = d_fcnds.ptr;
+        mv.fccls = d_fccls.ptr;
+        mv.clfcs = d_clfcs.ptr;
+        mv.cltpn = d_cltpn.ptr;
+
+        nslot = 0;
+        for (int64_t icl = 0; icl < ncell; ++icl)
+        {
+            int32_t const t = mesh.cltpn(icl);
+            bool ok = (ND == 2) ? (t == CT_TRIANGLE || t == CT_QUAD)
+                                : (t == CT_TET || t == CT_HEX || t == CT_PRISM || t == CT_PYRAMID);
+            if (!ok)
+            {
+                throw std::invalid_argument("EulerCore: cell " + std::to_string(icl) + " has type " +
+                                            std::to_string(t) + " unsupported in " + std::to_string(ND) + "D");
+            }
+            nslot = std::max(nslot, static_cast<int>(mesh.clfcs(icl, 0)));
+        }
+
+        // Solution state.
+        for (auto & r : rec)
+        {
+            r.alloc(static_cast<size_t>(nrow * RS));
+            cuda_check(cudaMemsetAsync(r.ptr, 0, r.bytes(), stream), "memset");
+        }
+        d_gamma.alloc(nrow);
+        d_cflo.alloc(nrow);
+        d_cflc.alloc(nrow);
+        d_limiter.alloc(std::max<int64_t>(ncell, 1));
+        cuda_check(cudaMemsetAsync(d_gamma.ptr, 0, d_gamma.bytes(), stream), "memset");
+        cuda_check(cudaMemsetAsync(d_cflo.ptr, 0, d_cflo.bytes(), stream), "memset");
+        cuda_check(cudaMemsetAsync(d_cflc.ptr, 0, d_cflc.bytes(), stream), "memset");
+        cuda_check(cudaMemsetAsync(d_limiter.ptr, 0, d_limiter.bytes(), stream), "memset");
+
+        // Boundary tables.
+        d_gkind.alloc(std::max<int64_t>(ngstcell, 1));
+        d_gnml.alloc(std::max<int64_t>(ngstcell * ND, 1));
+        d_gval.alloc(std::max<int64_t>(ngstcell * NEQ, 1));
+        d_gint.alloc(std::max<int64_t>(ngstcell, 1));
+
+        // Geometry: prepare_ce, then the compact march tables.
+        d_fgeo.alloc(static_cast<size_t>(std::max(nslot, 1)) * KF * std::max<int64_t>(ncell, 1));
+        d_cgeo.alloc(static_cast<size_t>(Dim<ND>::KC) * std::max<int64_t>(ncell, 1));
+        d_nbr.alloc(static_cast<size_t>(std::max(nslot, 1)) * std::max<int64_t>(ncell, 1));
+        d_ctype.alloc(std::max<int64_t>(ncell, 1));
+        prepare_ce(true);
+        upload_bc();
+        sync();
+    }
+
+    ~EulerCoreImpl() override
+    {
+        if (own_stream)
+        {
+            cudaStreamSynchronize(own_stream);
+            cudaStreamDestroy(own_stream);
+        }
+    }
+
+    size_t device_bytes() const override
+    {
+        size_t b = 0;
+        for (auto const & r : rec)
+            b += r.bytes();
+        b += d_fgeo.bytes() + d_cgeo.bytes() + d_nbr.bytes() + d_ctype.bytes();
+        b += d_gamma.bytes() + d_cflo.bytes() + d_cflc.bytes();
+        b += d_ndcrd.bytes() + d_fccnd.bytes() + d_clcnd.bytes() + d_fcnds.bytes() + d_fccls.bytes() +
+             d_clfcs.bytes() + d_cltpn.bytes() + d_clvol.bytes();
+        for (auto const & c : ce)
+            b += c.bytes();
+        return b;
+    }
+
+    void set_stream(cudaStream_t s) override
+    {
+        sync();
+        stream = s ? s : own_stream;
+    }
+
+    void sync() override { cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+
+    // ---- geometry -------------------------------------------------------
+
+    // (Re)compute the reference-layout CE tables into ce[] and compact them.
+    // When keep is false the big sub-face tables are released afterwards.
+    void prepare_ce(bool drop_subface)
+    {
+        int64_t const tot = nrow;
+        size_t const sz[4] = {static_cast<size_t>(tot * 7), static_cast<size_t>(tot * 7 * ND),
+                              static_cast<size_t>(ncell * 24 * ND), static_cast<size_t>(ncell * 24 * ND)};
+        for (int k = 0; k < 4; ++k)
+        {
+            if (ce[k].n != sz[k])
+            {
+                ce[k].alloc(sz[k]);
+            }
+            if (ce[k].ptr)
+            {
+                cuda_check(cudaMemsetAsync(ce[k].ptr, 0, ce[k].bytes(), stream), "memset");
+            }
+        }
+        if (ncell > 0)
+        {
+            CeView v{ce[0].ptr, ce[1].ptr, ce[2].ptr, ce[3].ptr};
+            if constexpr (ND == 2)
+                k_prepare_ce_2d<<<grid_for(ncell), BLOCK, 0, stream>>>(mv, v);
+            else
+                k_prepare_ce_3d<<<grid_for(ncell), BLOCK, 0, stream>>>(mv, v);
+            launched(stream, "prepare_ce");
+        }
+        compact();
+        if (drop_subface)
+        {
+            sync();
+            ce[2].release();
+            ce[3].release();
+        }
+    }
+
+    void ensure_ce()
+    {
+        if (!ce[2].ptr && ncell > 0)
+        {
+            // Recompute the sub-face tables without touching cevol/cecnd,
+            // which the caller may have overwritten.
+            DevBuf<double> t0(static_cast<size_t>(nrow * 7)), t1(static_cast<size_t>(nrow * 7 * ND));
+            ce[2].alloc(static_cast<size_t>(ncell * 24 * ND));
+            ce[3].alloc(static_cast<size_t>(ncell * 24 * ND));
+            cuda_check(cudaMemsetAsync(ce[2].ptr, 0, ce[2].bytes(), stream), "memset");
+            cuda_check(cudaMemsetAsync(ce[3].ptr, 0, ce[3].bytes(), stream), "memset");
+            CeView v{t0.ptr, t1.ptr, ce[2].ptr, ce[3].ptr};
+            if constexpr (ND == 2)
+                k_prepare_ce_2d<<<grid_for(ncell), BLOCK, 0, stream>>>(mv, v);
+            else
+                k_prepare_ce_3d<<<grid_for(ncell), BLOCK, 0, stream>>>(mv, v);
+            launched(stream, "prepare_ce");
+            sync();
+        }
+    }
+
+    void compact()
+    {
+        if (ncell == 0)
+        {
+            return;
+        }
+        ensure_ce();
+        k_compact<ND, G><<<grid_for(ncell), BLOCK, 0, stream>>>(mv, ce[0].ptr, ce[1].ptr, ce[2].ptr, ce[3].ptr,
+                                                                0.5 * time_increment, std::max(nslot, 1),
+                                                                d_fgeo.ptr, d_cgeo.ptr, d_nbr.ptr, d_ctype.ptr);
+        launched(stream, "compact");
+    }
+
+    // ---- boundary conditions ---------------------------------------------
+
+    void upload_bc()
+    {
+        if (!m_bc_dirty)
+        {
+            return;
+        }
+        std::vector<int8_t> kind(static_cast<size_t>(ngstcell), -1);
+        std::vector<double> nml(static_cast<size_t>(ngstcell * ND), 0.0);
+        std::vector<double> val(static_cast<size_t>(ngstcell * NEQ), 0.0);
+        std::vector<int32_t> gint(static_cast<size_t>(ngstcell), 0);
+        // Later registrations override earlier ones for a face, as the
+        // reference's sequential trim passes do.
+        for (auto const & b : m_bcs)
+        {
+            double st[NEQ] = {};
+            if (b.kind == BC_INLET)
+            {
+                double const rho = b.value[0];
+                double const p = b.value[1 + ND];
+                double const ga = b.value[2 + ND];
+                double vsq = 0.0;
+                for (int d = 0; d < ND; ++d)
+                {
+                    vsq += b.value[1 + d] * b.value[1 + d];
+                }
+                st[0] = rho;
+                for (int d = 0; d < ND; ++d)
+                {
+                    st[1 + d] = rho * b.value[1 + d];
+                }
+                st[NEQ - 1] = p / (ga - 1.0) + 0.5 * rho * vsq;
+            }
+            for (int32_t const ifc : b.faces)
+            {
+                int32_t const icl = m_fccls[static_cast<size_t>((ifc + m_ngstface) * 4 + 0)];
+                int32_t const jcl = m_fccls[static_cast<size_t>((ifc + m_ngstface) * 4 + 1)];
+                int64_t const g = jcl + ngstcell;
+                if (g < 0 || g >= ngstcell)
+                {
+                    throw std::runtime_error("EulerCore: boundary face " + std::to_string(ifc) +
+                                             " has no ghost cell; build the ghost layer first");
+                }
+                kind[g] = static_cast<int8_t>(b.kind);
+                gint[g] = static_cast<int32_t>(icl + ngstcell);
+                for (int d = 0; d < ND; ++d)
+                {
+                    nml[g * ND + d] = m_fcnml[static_cast<size_t>((ifc + m_ngstface) * ND + d)];
+                }
+                for (int i = 0; i < NEQ; ++i)
+                {
+                    val[g * NEQ + i] = st[i];
+                }
+            }
+        }
+        if (ngstcell > 0)
+        {
+            h2d(d_gkind.ptr, kind.data(), kind.size());
+            h2d(d_gnml.ptr, nml.data(), nml.size());
+            h2d(d_gval.ptr, val.data(), val.size());
+            h2d(d_gint.ptr, gint.data(), gint.size());
+            sync();
+        }
+        m_bc_dirty = false;
+        next_valid = false;
+    }
+
+    // ---- state access ----------------------------------------------------
+
+    MarchArgs<R, G> args()
+    {
+        MarchArgs<R, G> a{};
+        a.cur = rec[cur].ptr;
+        a.nxt = rec[cur ^ 1].ptr;
+        a.gamma = d_gamma.ptr;
+        a.cflo = d_cflo.ptr;
+        a.cflc = d_cflc.ptr;
+        a.fgeo = d_fgeo.ptr;
+        a.cgeo = d_cgeo.ptr;
+        a.nbr = d_nbr.ptr;
+        a.ctype = d_ctype.ptr;
+        a.gkind = d_gkind.ptr;
+        a.gnml = d_gnml.ptr;
+        a.gval = d_gval.ptr;
+        a.limiter = d_limiter.ptr;
+        a.ncell = ncell;
+        a.ngst = ngstcell;
+        a.dt = R(time_increment);
+        a.hdt = R(time_increment * 0.5);
+        a.qdt = R(time_increment * 0.25);
+        a.sigma0 = R(sigma0);
+        a.taumin = R(taumin);
+        a.tauscale = R(tauscale);
+        return a;
+    }
+
+    void field_of(int which, R *& base, int & off, int & width)
+    {
+        switch (which)
+        {
+        case EA_SO0C: base = rec[cur].ptr; off = 0; width = NEQ; break;
+        case EA_SO0N: base = rec[cur ^ 1].ptr; off = 0; width = NEQ; break;
+        case EA_SO0T: base = rec[tbuf].ptr; off = NEQ; width = NEQ; break;
+        case EA_SO1C: base = rec[cur].ptr; off = 2 * NEQ; width = NEQ * ND; break;
+        case EA_SO1N: base = rec[cur ^ 1].ptr; off = 2 * NEQ; width = NEQ * ND; break;
+        default: throw std::invalid_argument("not a record field");
+        }
+    }
+
+    void get_array(int which, double * out) override
+    {
+        upload_bc();
+        int64_t const n = array_size(which);
+        if (which == EA_STM)
+        {
+            std::memcpy(out, m_stm.data(), sizeof(double) * static_cast<size_t>(n));
+            return;
+        }
+        if (n == 0)
+        {
+            return;
+        }
+        DevBuf<double> tmp(static_cast<size_t>(n));
+        if (which >= EA_CEVOL && which <= EA_SFNML)
+        {
+            ensure_ce();
+            cuda_check(cudaMemcpyAsync(tmp.ptr, ce[which].ptr, tmp.bytes(), cudaMemcpyDeviceToDevice, stream), "copy");
+        }
+        else if (which == EA_CFLO || which == EA_CFLC || which == EA_GAMMA)
+        {
+            R const * src = which == EA_CFLO ? d_cflo.ptr : which == EA_CFLC ? d_cflc.ptr : d_gamma.ptr;
+            k_to_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(src, tmp.ptr, n);
+            launched(stream, "to_f64");
+        }
+        else
+        {
+            R * base;
+            int off, width;
+            field_of(which, base, off, width);
+            k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp.ptr, nrow, off, width);
+            launched(stream, "get_field");
+        }
+        cuda_check(cudaMemcpyAsync(out, tmp.ptr, tmp.bytes(), cudaMemcpyDeviceToHost, stream), "D2H");
+        sync();
+    }
+
+    void set_array(int which, double const * in) override
+    {
+        upload_bc();
+        int64_t const n = array_size(which);
+        if (which == EA_STM)
+        {
+            std::memcpy(m_stm.data(), in, sizeof(double) * static_cast<size_t>(n));
+            return;
+        }
+        if (n == 0)
+        {
+            return;
+        }
+        DevBuf<double> tmp(static_cast<size_t>(n));
+        cuda_check(cudaMemcpyAsync(tmp.ptr, in, tmp.bytes(), cudaMemcpyHostToDevice, stream), "H2D");
+        if (which >= EA_CEVOL && which <= EA_SFNML)
+        {
+            ensure_ce();
+            cuda_check(cudaMemcpyAsync(ce[which].ptr, tmp.ptr, tmp.bytes(), cudaMemcpyDeviceToDevice, stream), "copy");
+            compact();
+        }
+        else if (which == EA_CFLO || which == EA_CFLC || which == EA_GAMMA)
+        {
+            R * dst = which == EA_CFLO ? d_cflo.ptr : which == EA_CFLC ? d_cflc.ptr : d_gamma.ptr;
+            k_from_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(tmp.ptr, dst, n);
+            launched(stream, "from_f64");
+        }
+        else
+        {
+            R * base;
+            int off, width;
+            field_of(which, base, off, width);
+            k_set_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp.ptr, nrow, off, width);
+            launched(stream, "set_field");
+        }
+        next_valid = false;
+        sync();
+    }
+
+    void init_solution(double gamma, double rho, double const * v, double p) override
+    {
+        if (gamma <= 1.0)
+        {
+            throw std::invalid_argument("EulerCore::init_solution: gamma " + std::to_string(gamma) + " must be > 1");
+        }
+        if (rho <= 0.0)
+        {
+            throw std::invalid_argument("EulerCore::init_solution: rho " + std::to_string(rho) + " must be > 0");
+        }
+        if (p < 0.0)
+        {
+            throw std::invalid_argument("EulerCore::init_solution: pressure " + std::to_string(p) +
+                                        " must be >= 0");
+        }
+        double vsq = 0.0;
+        for (int d = 0; d < ND; ++d)
+        {
+            vsq += v[d] * v[d];
+        }
+        double const energy = p / (gamma - 1.0) + 0.5 * rho * vsq;
+        if (nrow > 0)
+        {
+            k_init<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_gamma.ptr, ngstcell, nrow, gamma,
+                                                                 rho, rho * v[0], rho * v[1],
+                                                                 ND == 3 ? rho * v[2] : 0.0, energy);
+            launched(stream, "init_solution");
+        }
+        next_valid = false;
+        sync();
+    }
+
+    // ---- operations ------------------------------------------------------
+
+    // Make rec[cur].so0t the logical so0t (copy it over if update() moved
+    // the current buffer away from it).
+    void so0t_to_cur()
+    {
+        if (tbuf != cur)
+        {
+            k_copy_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(rec[tbuf].ptr, rec[cur].ptr, nrow, NEQ, NEQ);
+            launched(stream, "copy_so0t");
+            tbuf = cur;
+        }
+    }
+
+    void run_solt()
+    {
+        k_solt_rows<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(rec[cur].ptr, d_gamma.ptr, nrow);
+        launched(stream, "calc_solt");
+        tbuf = cur;
+    }
+
+    void op(int which) override
+    {
+        upload_bc();
+        bool const has_cells = ncell > 0;
+        switch (which)
+        {
+        case EO_PREPARE_CE:
+            prepare_ce(false);
+            break;
+        case EO_UPDATE:
+            cur ^= 1;
+            break;
+        case EO_CALC_SOLT:
+            if (nrow > 0)
+                run_solt();
+            next_valid = false;
+            break;
+        case EO_CALC_SOLN:
+            so0t_to_cur();
+            if (has_cells)
+            {
+                k_soln<ND, R, G><<<grid_for(ncell), BLOCK, 0, stream>>>(args());
+                launched(stream, "calc_soln");
+            }
+            next_valid = false;
+            break;
+        case EO_BC_SOLN:
+            if (ngstcell > 0)
+            {
+                k_bc0<ND, R, G><<<grid_for(ngstcell), BLOCK, 0, stream>>>(args(), d_gint.ptr);
+                launched(stream, "bc_soln");
+            }
+            next_valid = false;
+            break;
+        case EO_CALC_CFL:
+            if (has_cells)
+            {
+                k_cfl<ND, R, G><<<grid_for(ncell), BLOCK, 0, stream>>>(args());
+                launched(stream, "calc_cfl");
+            }
+            next_valid = false;
+            break;
+        case EO_CALC_DSOLN:
+            so0t_to_cur();
+            if (has_cells)
+            {
+                k_dsoln<ND, R, G><<<grid_for(ncell), BLOCK, 0, stream>>>(args());
+                launched(stream, "calc_dsoln");
+            }
+            next_valid = false;
+            break;
+        case EO_BC_DSOLN:
+            if (ngstcell > 0)
+            {
+                k_bc1<ND, R, G><<<grid_for(ngstcell), BLOCK, 0, stream>>>(args(), d_gint.ptr);
+                launched(stream, "bc_dsoln");
+            }
+            next_valid = false;
+            break;
+        case EO_MARCH_SUBSTEP:
+            march_substep();
+            break;
+        default:
+            throw std::invalid_argument("EulerCore: unknown operation " + std::to_string(which));
+        }
+        sync();
+    }
+
+    // march_substep (euler_march.cpp:339-348) as update() plus one fused
+    // kernel; calc_solt runs only when the previous fused kernel did not
+    // already leave it in the new current buffer.
+    void march_substep()
+    {
+        cur ^= 1;
+        if (next_valid && next_buf == cur)
+        {
+            tbuf = cur;
+        }
+        else if (nrow > 0)
+        {
+            run_solt();
+        }
+        if (nrow > 0)
+        {
+            k_fused<ND, R, G><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            launched(stream, "fused_substep");
+            next_valid = true;
+            next_buf = cur ^ 1;
+        }
+    }
+
+    void march(int64_t steps) override
+    {
+        upload_bc();
+        for (int64_t s = 0; s < steps; ++s)
+        {
+            march_substep();
+            march_substep();
+        }
+    }
+
+    void limiter_mask(uint8_t * out) override
+    {
+        if (ncell > 0)
+        {
+            cuda_check(cudaMemcpyAsync(out, d_limiter.ptr, static_cast<size_t>(ncell), cudaMemcpyDeviceToHost, stream),
+                       "D2H");
+        }
+        sync();
+    }
+
+    void reduce(double * part_out, int & nblk)
+    {
+        nblk = static_cast<int>(std::min<int64_t>(std::max<int64_t>(grid_for(ncell), 1), 1024));
+        DevBuf<double> part(static_cast<size_t>(nblk * (NEQ + 2)));
+        k_totals<ND, R><<<nblk, BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_clvol.ptr, d_cflo.ptr, ngstcell, ncell,
+                                                   part.ptr);
+        launched(stream, "totals");
+        std::vector<double> h(static_cast<size_t>(nblk * (NEQ + 2)));
+        cuda_check(cudaMemcpyAsync(h.data(), part.ptr, part.bytes(), cudaMemcpyDeviceToHost, stream), "D2H");
+        sync();
+        for (int i = 0; i < NEQ + 2; ++i)
+        {
+            part_out[i] = 0.0;
+        }
+        double c[NEQ] = {};
+        part_out[NEQ] = 1.79769313486231570815e+308;
+        part_out[NEQ + 1] = -1.79769313486231570815e+308;
+        for (int b = 0; b < nblk; ++b)
+        {
+            for (int i = 0; i < NEQ; ++i)
+            {
+                double const y = h[static_cast<size_t>(b * (NEQ + 2) + i)] - c[i];
+                double const t = part_out[i] + y;
+                c[i] = (t - part_out[i]) - y;
+                part_out[i] = t;
+            }
+            part_out[NEQ] = std::fmin(part_out[NEQ], h[static_cast<size_t>(b * (NEQ + 2) + NEQ)]);
+            part_out[NEQ + 1] = std::fmax(part_out[NEQ + 1], h[static_cast<size_t>(b * (NEQ + 2) + NEQ + 1)]);
+        }
+    }
+
+    void totals(double * out) override
+    {
+        double p[NEQ + 2];
+        int nb = 0;
+        reduce(p, nb);
+        for (int i = 0; i < NEQ; ++i)
+        {
+            out[i] = p[i];
+        }
+    }
+
+    void cfl_range(double * out) override
+    {
+        double p[NEQ + 2];
+        int nb = 0;
+        reduce(p, nb);
+        out[0] = p[NEQ];
+        out[1] = p[NEQ + 1];
+    }
+
+private:
+    template <typename T>
+    void up(DevBuf<T> & d, std::vector<T> const & h)
+    {
+        d.alloc(std::max<size_t>(h.size(), 1));
+        if (!h.empty())
+        {
+            h2d(d.ptr, h.data(), h.size());
+        }
+    }
+
+    template <typename T>
+    void h2d(T * dst, T const * src, size_t n)
+    {
+        cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, stream), "H2D");
+        cuda_check(cudaStreamSynchronize(stream), "sync");
+    }
+
+    int64_t nrow = 0;
+    int nslot = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    MeshView mv{};
+
+    DevBuf<double> d_ndcrd, d_fccnd, d_clcnd, d_clvol;
+    DevBuf<int32_t> d_fcnds, d_fccls, d_clfcs, d_cltpn;
+    DevBuf<double> ce[4]; // cevol, cecnd, sfcnd, sfnml (reference layout)
+    DevBuf<G> d_fgeo, d_cgeo;
+    DevBuf<int32_t> d_nbr;
+    DevBuf<int8_t> d_ctype;
+    DevBuf<R> rec[2];
+    DevBuf<R> d_gamma, d_cflo, d_cflc;
+    DevBuf<uint8_t> d_limiter;
+    DevBuf<int8_t> d_gkind;
+    DevBuf<double> d_gnml, d_gval;
+    DevBuf<int32_t> d_gint;
+
+    int cur = 0;           // index of the current (so0c/so1c) record buffer
+    int tbuf = 0;          // buffer holding the logical so0t
+    bool next_valid = false; // rec[next_buf].so0t == calc_solt of rec[next_buf]
+    int next_buf = 1;
+};
+
+} // namespace
+
+std::unique_ptr<EulerCoreBase> make_euler_core(HostMesh const & mesh, double dt, int prec)
+{
+    if (mesh.ngstcell != mesh.nbound)
+    {
+        throw std::invalid_argument("EulerCore: the mesh needs build_boundary() and build_ghost() first");
+    }
+    if (prec < PREC_FP64 || prec > PREC_FP32)
+    {
+        throw std::invalid_argument("EulerCore: unknown precision " + std::to_string(prec));
+    }
+    if (mesh.ndim == 2)
+    {
+        if (prec == PREC_FP64)
+            return std::make_unique<EulerCoreImpl<2, double, double>>(mesh, dt, prec);
+        if (prec == PREC_FP32_GEOM64)
+            return std::make_unique<EulerCoreImpl<2, float, double>>(mesh, dt, prec);
+        return std::make_unique<EulerCoreImpl<2, float, float>>(mesh, dt, prec);
+    }
+    if (prec == PREC_FP64)
+        return std::make_unique<EulerCoreImpl<3, double, double>>(mesh, dt, prec);
+    if (prec == PREC_FP32_GEOM64)
+        return std::make_unique<EulerCoreImpl<3, float, double>>(mesh, dt, prec);
+    return std::make_unique<EulerCoreImpl<3, float, float>>(mesh, dt, prec);
+}
+
+} // namespace scg

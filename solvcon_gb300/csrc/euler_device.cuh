@@ -1,0 +1,328 @@
+#pragma once
+
+/*
+ * Device-side building blocks of the multi-dimensional CESE Euler march.
+ *
+ * The arithmetic is that of the reference EulerCore (cpp/solvcon/multidim/
+ * euler_march.cpp, euler_solution.cpp, euler_gradient.cpp, euler_bc.cpp,
+ * GradientElement.cpp) rearranged for a GPU whose FP64 pipe, not its HBM, is
+ * the scarce resource:
+ *
+ *  - The flux Jacobian is never formed.  Every product J_d(u) . w the
+ *    reference takes (euler_march.cpp:178-189, 280-292) is the directional
+ *    derivative of the Euler flux f_d at u along w, evaluated here directly from
+ *    primitive variables (jvp_sum).  Same mathematics, about a third of the
+ *    operations.
+ *  - The sub-face loop of calc_soln (euler_march.cpp:266-294) is linear in the
+ *    sub-face centroids and normals, so each face's sub-faces are folded into
+ *    two geometric moments at set-up: N = sum_sf n_sf and
+ *    M[e][d] = sum_sf (x_sf - x_j)[e] n_sf[d] (pre-scaled by dt/2).
+ *  - The gradient element (GradientElement.cpp:305-381) is linear in tau, so
+ *    its displacement vectors are idis = P + tau Q - delta and
+ *    jdis = R + tau Q - delta with P, Q, R precomputed per face; for simplices
+ *    the sub-element centroid shift delta is exactly zero (the fan of a
+ *    simplex about its vertex mean has equal sub-volumes).
+ *  - Each fundamental gradient element's 2x2/3x3 solve
+ *    (GradientElement.cpp:447-458) uses its inverse's rows once per cell,
+ *    instead of an adjugate and determinant per equation.
+ *
+ * Results equal the reference's up to floating-point round-off.
+ *
+ * Storage (one record per mesh row, ghost rows first, row = icl + ngstcell):
+ *   record[row] = { so0[NEQ], so0t[NEQ], so1[NEQ][ND] } padded to RS reals.
+ */
+
+#include <cstdint>
+
+namespace scg
+{
+namespace dev
+{
+
+template <int ND>
+struct Dim
+{
+    static constexpr int NEQ = ND + 2;
+    static constexpr int RS = (ND == 2) ? 16 : 32; // record stride in reals
+    static constexpr int OT = NEQ;                 // so0t offset
+    static constexpr int O1 = 2 * NEQ;             // so1 offset
+    // Face geometry components: bvol, dB[ND], Nh[ND], Mh[ND][ND], P[ND], Q[ND], R[ND].
+    static constexpr int K_BVOL = 0;
+    static constexpr int K_DB = 1;
+    static constexpr int K_NH = 1 + ND;
+    static constexpr int K_MH = 1 + 2 * ND;
+    static constexpr int K_P = 1 + 2 * ND + ND * ND;
+    static constexpr int K_Q = K_P + ND;
+    static constexpr int K_R = K_Q + ND;
+    static constexpr int KF = K_R + ND;
+    // Cell geometry components: 1/cevol[0], hdt/dist.
+    static constexpr int KC = 2;
+};
+
+// Small constants of the reference, with FP32-safe floors.  The FP64 values
+// are the reference's own (euler_march.cpp:30, euler_solution.cpp:242,
+// euler_gradient.cpp:28); 1e-60 and 1e-200 underflow in FP32, so the FP32
+// march uses the smallest floors that keep the same expressions finite.
+template <typename R>
+struct Tiny;
+template <>
+struct Tiny<double>
+{
+    static constexpr double JAC = 1.e-60;
+    static constexpr double CFL = 1.e-60;
+    static constexpr double AZ = 1.e-200;
+};
+template <>
+struct Tiny<float>
+{
+    static constexpr float JAC = 1.e-30f;
+    static constexpr float CFL = 1.e-30f;
+    static constexpr float AZ = 1.e-37f;
+};
+
+// Reciprocal square root: the library routine for each precision.
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double sqr_t(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqr_t(float x) { return sqrtf(x); }
+
+// Compensated (Kahan) accumulator for the FP32 flux sums; plain sum in FP64.
+template <typename R>
+struct Acc
+{
+    R s = R(0);
+    __device__ __forceinline__ void add(R x) { s += x; }
+    __device__ __forceinline__ R value() const { return s; }
+};
+template <>
+struct Acc<float>
+{
+    float s = 0.f;
+    float c = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        float const y = x - c;
+        float const t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s; }
+};
+
+// Primitive quantities of a conserved state u (with the reference's density
+// floor TINY, euler_march.cpp:41).
+template <int ND, typename R>
+struct Prim
+{
+    R r;     // 1 / (rho + TINY)
+    R v[ND]; // velocity
+    R p;     // pressure
+    R h;     // E + p
+    R ga1;   // gamma - 1
+    R vsq;   // |v|^2
+
+    __device__ __forceinline__ Prim(R const * u, R ga)
+    {
+        constexpr int NEQ = ND + 2;
+        r = R(1) / (u[0] + Tiny<R>::JAC);
+        R ke2 = R(0);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            v[d] = u[1 + d] * r;
+            ke2 += u[1 + d] * v[d];
+        }
+        vsq = ke2 * r;
+        ga1 = ga - R(1);
+        p = ga1 * (u[NEQ - 1] - R(0.5) * ke2);
+        h = u[NEQ - 1] + p;
+    }
+};
+
+// out[i] = sum_d f_d(u)[i] * n[d]  (the flux of euler_march.cpp:58-61, 120-124).
+template <int ND, typename R>
+__device__ __forceinline__ void flux_dot(Prim<ND, R> const & q, R const * u, R const * n, R * out)
+{
+    constexpr int NEQ = ND + 2;
+    R mn = R(0);
+    R vn = R(0);
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        mn += u[1 + d] * n[d];
+        vn += q.v[d] * n[d];
+    }
+    out[0] = mn;
+#pragma unroll
+    for (int k = 0; k < ND; ++k)
+    {
+        out[1 + k] = u[1 + k] * vn + q.p * n[k];
+    }
+    out[NEQ - 1] = q.h * vn;
+}
+
+// out[i] += sum_d (J_d(u) . w[:, d])[i], with w indexed w[i * ND + d].  J_d is
+// the analytic Euler flux Jacobian of euler_march.cpp:63-81 / 126-156; its
+// product with w is taken as the directional derivative of f_d.
+template <int ND, typename R>
+__device__ __forceinline__ void jvp_sum(Prim<ND, R> const & q, R const * u, R const * w, R * out)
+{
+    constexpr int NEQ = ND + 2;
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        R const w0 = w[0 * ND + d];
+        R const we = w[(NEQ - 1) * ND + d];
+        R vw = R(0);
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+        {
+            vw += q.v[k] * w[(1 + k) * ND + d];
+        }
+        R const dp = q.ga1 * (we - vw + R(0.5) * q.vsq * w0);
+        R const dvd = (w[(1 + d) * ND + d] - q.v[d] * w0) * q.r;
+        out[0] += w[(1 + d) * ND + d];
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+        {
+            out[1 + k] += w[(1 + k) * ND + d] * q.v[d] + u[1 + k] * dvd;
+        }
+        out[1 + d] += dp;
+        out[NEQ - 1] += (we + dp) * q.v[d] + q.h * dvd;
+    }
+}
+
+// so0t = -(J . so1) for one row (euler_march.cpp:160-191).
+template <int ND, typename R>
+__device__ __forceinline__ void solt_row(R const * u, R const * g, R ga, R * t)
+{
+    constexpr int NEQ = ND + 2;
+    Prim<ND, R> const q(u, ga);
+    R o[NEQ];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        o[i] = R(0);
+    }
+    jvp_sum<ND, R>(q, u, g, o);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        t[i] = -o[i];
+    }
+}
+
+// Fundamental gradient element tables (1-based in GradientElement.cpp:
+// 184-247, 0-based here), per cell type.
+template <int CT>
+struct CellT;
+
+template <>
+struct CellT<4> // triangle
+{
+    static constexpr int ND = 2, NFC = 3, NFGE = 3;
+    static constexpr bool SIMPLEX = true;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+        return t[k][v];
+    }
+};
+template <>
+struct CellT<3> // quadrilateral
+{
+    static constexpr int ND = 2, NFC = 4, NFGE = 4;
+    static constexpr bool SIMPLEX = false;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+        return t[k][v];
+    }
+};
+template <>
+struct CellT<6> // tetrahedron
+{
+    static constexpr int ND = 3, NFC = 4, NFGE = 4;
+    static constexpr bool SIMPLEX = true;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[4][3] = {{2, 0, 1}, {1, 0, 3}, {3, 0, 2}, {1, 3, 2}};
+        return t[k][v];
+    }
+};
+template <>
+struct CellT<5> // hexahedron
+{
+    static constexpr int ND = 3, NFC = 6, NFGE = 8;
+    static constexpr bool SIMPLEX = false;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[8][3] = {{1, 2, 4}, {5, 2, 1}, {3, 2, 5}, {4, 2, 3},
+                                 {4, 0, 1}, {1, 0, 5}, {5, 0, 3}, {3, 0, 4}};
+        return t[k][v];
+    }
+};
+template <>
+struct CellT<7> // prism
+{
+    static constexpr int ND = 3, NFC = 5, NFGE = 6;
+    static constexpr bool SIMPLEX = false;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[6][3] = {{4, 1, 3}, {2, 1, 4}, {3, 1, 2}, {3, 0, 4}, {4, 0, 2}, {2, 0, 3}};
+        return t[k][v];
+    }
+};
+template <>
+struct CellT<8> // pyramid
+{
+    static constexpr int ND = 3, NFC = 5, NFGE = 6;
+    static constexpr bool SIMPLEX = false;
+    __device__ static constexpr int fge(int k, int v)
+    {
+        constexpr int t[6][3] = {{0, 4, 1}, {1, 4, 2}, {2, 4, 3}, {3, 4, 0}, {0, 2, 3}, {2, 0, 1}};
+        return t[k][v];
+    }
+};
+
+// Determinant of the rows a, b (, c).
+template <int ND, typename R>
+__device__ __forceinline__ R det_rows(R const * a, R const * b, R const * c)
+{
+    if constexpr (ND == 2)
+    {
+        (void)c;
+        return a[0] * b[1] - a[1] * b[0];
+    }
+    else
+    {
+        return a[0] * (b[1] * c[2] - b[2] * c[1]) - a[1] * (b[0] * c[2] - b[2] * c[0]) +
+               a[2] * (b[0] * c[1] - b[1] * c[0]);
+    }
+}
+
+// Kernel argument block shared by the march kernels.
+template <typename R, typename G>
+struct MarchArgs
+{
+    R const * cur;        // current records (so0c, so0t, so1c)
+    R * nxt;              // new records (so0n, next so0t, so1n)
+    R const * gamma;      // [nrow]
+    R * cflo;             // [nrow]
+    R * cflc;             // [nrow]
+    G const * fgeo;       // [NSLOT][KF][ncell]
+    G const * cgeo;       // [KC][ncell]
+    int32_t const * nbr;  // [NSLOT][ncell] neighbour row
+    int8_t const * ctype; // [ncell]
+    int8_t const * gkind; // [ngst] BC kind of the ghost row, -1 if none
+    double const * gnml;  // [ngst][ND] outward unit normal of the boundary face
+    double const * gval;  // [ngst][NEQ] inlet conserved state
+    uint8_t * limiter;    // [ncell] W-3/4 firing bits per equation, or null
+    int64_t ncell;
+    int64_t ngst;
+    R dt, hdt, qdt;
+    R sigma0, taumin, tauscale;
+};
+
+} // namespace dev
+} // namespace scg

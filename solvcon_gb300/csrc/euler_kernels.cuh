@@ -1,0 +1,688 @@
+#pragma once
+
+/*
+ * The CESE march kernels of the multi-dimensional Euler core: per-cell device
+ * routines for calc_soln, bc_soln, calc_cfl, calc_dsoln, bc_dsoln and calc_solt,
+ * the fused one-kernel substep built from them, and the set-up kernels
+ * (prepare_ce and the geometry compaction).  See euler_device.cuh for the data
+ * layout and for how the arithmetic relates to the reference's.
+ */
+
+#include "euler_device.cuh"
+
+namespace scg
+{
+namespace dev
+{
+
+template <typename T>
+__device__ __forceinline__ T ldg(T const * p)
+{
+    return __ldg(p);
+}
+
+// Load the used part of a record (so0, so0t, so1).
+template <int ND, typename R>
+__device__ __forceinline__ void load_rec(R const * base, R * out)
+{
+    constexpr int N = 2 * (ND + 2) + (ND + 2) * ND; // 16 (2D) or 25 (3D)
+    if constexpr (sizeof(R) == 8)
+    {
+        double2 const * p = reinterpret_cast<double2 const *>(base);
+#pragma unroll
+        for (int k = 0; k < N / 2; ++k)
+        {
+            double2 const v = __ldg(p + k);
+            out[2 * k] = v.x;
+            out[2 * k + 1] = v.y;
+        }
+        if constexpr (N % 2)
+        {
+            out[N - 1] = __ldg(base + N - 1);
+        }
+    }
+    else
+    {
+        float4 const * p = reinterpret_cast<float4 const *>(base);
+#pragma unroll
+        for (int k = 0; k < N / 4; ++k)
+        {
+            float4 const v = __ldg(p + k);
+            out[4 * k] = v.x;
+            out[4 * k + 1] = v.y;
+            out[4 * k + 2] = v.z;
+            out[4 * k + 3] = v.w;
+        }
+#pragma unroll
+        for (int k = (N / 4) * 4; k < N; ++k)
+        {
+            out[k] = __ldg(base + k);
+        }
+    }
+}
+
+// Store the used part of a record (so0, so0t, so1).
+template <int ND, typename R>
+__device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0t, R const * so1)
+{
+    constexpr int NEQ = ND + 2;
+    constexpr int N = 2 * NEQ + NEQ * ND;
+    R v[N];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        v[i] = so0[i];
+        v[NEQ + i] = so0t[i];
+    }
+#pragma unroll
+    for (int i = 0; i < NEQ * ND; ++i)
+    {
+        v[2 * NEQ + i] = so1[i];
+    }
+    if constexpr (sizeof(R) == 8)
+    {
+        double2 * p = reinterpret_cast<double2 *>(base);
+#pragma unroll
+        for (int k = 0; k < N / 2; ++k)
+        {
+            p[k] = make_double2(v[2 * k], v[2 * k + 1]);
+        }
+        if constexpr (N % 2)
+        {
+            base[N - 1] = v[N - 1];
+        }
+    }
+    else
+    {
+        float4 * p = reinterpret_cast<float4 *>(base);
+#pragma unroll
+        for (int k = 0; k < N / 4; ++k)
+        {
+            p[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        }
+#pragma unroll
+        for (int k = (N / 4) * 4; k < N; ++k)
+        {
+            base[k] = v[k];
+        }
+    }
+}
+
+template <int ND, typename R, typename G>
+__device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t icl)
+{
+    return R(ldg(a.fgeo + (static_cast<int64_t>(f) * Dim<ND>::KF + k) * a.ncell + icl));
+}
+
+// ---------------------------------------------------------------------------
+// calc_soln for one body cell (euler_march.cpp:197-303): the CESE flux
+// integral over the cell's BCEs, divided by the CCE volume.  For simplices it
+// also returns, per face and equation, the two halves of the gradient
+// element's solution deltas that need only neighbour data:
+//   alpha = so0c + hdt so0t + R . so1c,   beta = Q . so1c
+// so that calc_dsoln needs no second gather.
+template <int CT, typename R, typename G, bool AB>
+__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n, R * alpha, R * beta)
+{
+    constexpr int ND = CellT<CT>::ND;
+    constexpr int NEQ = ND + 2;
+    constexpr int NFC = CellT<CT>::NFC;
+    using D = Dim<ND>;
+    Acc<R> acc[NEQ];
+#pragma unroll
+    for (int f = 0; f < NFC; ++f)
+    {
+        int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
+        R rec[2 * NEQ + NEQ * ND];
+        load_rec<ND, R>(a.cur + jr * D::RS, rec);
+        R const * u = rec;
+        R const * t = rec + NEQ;
+        R const * g = rec + 2 * NEQ;
+        R const ga = ldg(a.gamma + jr);
+
+        R const bvol = fg<ND>(a, f, D::K_BVOL, icl);
+        R dB[ND], nh[ND], qn[ND];
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            dB[d] = fg<ND>(a, f, D::K_DB + d, icl);
+            nh[d] = fg<ND>(a, f, D::K_NH + d, icl);
+            qn[d] = a.qdt * nh[d];
+        }
+        // Spatial flux: neighbour solution at the BCE centroid times its volume.
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i)
+        {
+            R s = u[i];
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                s += dB[d] * g[i * ND + d];
+            }
+            acc[i].add(s * bvol);
+        }
+        // Temporal flux: sum over sub-faces folded into Nh and Mh.
+        R w[NEQ * ND];
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                R s = t[i] * qn[d];
+#pragma unroll
+                for (int e = 0; e < ND; ++e)
+                {
+                    s += g[i * ND + e] * fg<ND>(a, f, D::K_MH + e * ND + d, icl);
+                }
+                w[i * ND + d] = s;
+            }
+        }
+        Prim<ND, R> const q(u, ga);
+        R fl[NEQ];
+        flux_dot<ND, R>(q, u, nh, fl);
+        jvp_sum<ND, R>(q, u, w, fl);
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i)
+        {
+            acc[i].add(-fl[i]);
+        }
+        if constexpr (AB)
+        {
+            R rr[ND], qq[ND];
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                rr[d] = fg<ND>(a, f, D::K_R + d, icl);
+                qq[d] = fg<ND>(a, f, D::K_Q + d, icl);
+            }
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                R al = u[i] + a.hdt * t[i];
+                R be = R(0);
+#pragma unroll
+                for (int d = 0; d < ND; ++d)
+                {
+                    al += rr[d] * g[i * ND + d];
+                    be += qq[d] * g[i * ND + d];
+                }
+                alpha[f * NEQ + i] = al;
+                beta[f * NEQ + i] = be;
+            }
+        }
+    }
+    R const ivol = R(ldg(a.cgeo + 0 * a.ncell + icl));
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        so0n[i] = acc[i].value() * ivol;
+    }
+}
+
+// calc_cfl for one body cell (euler_solution.cpp:240-294): original and
+// clamped CFL, and the energy rewritten from the non-negative pressure.
+template <int ND, typename R, typename G>
+__device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, int64_t row, R * so0n)
+{
+    constexpr int NEQ = ND + 2;
+    R const ga = ldg(a.gamma + row);
+    R const ga1 = ga - R(1);
+    R const rho = so0n[0];
+    R momsq = R(0);
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        momsq += so0n[1 + d] * so0n[1 + d];
+    }
+    R const ke = momsq / (R(2) * rho);
+    R const pr = ga1 * (so0n[NEQ - 1] - ke);
+    R const pra = (pr + fabs(pr)) / R(2);
+    R const wspd = sqr_t(ga * pra / rho) + sqr_t(momsq) / rho;
+    R const cflo = wspd * R(ldg(a.cgeo + 1 * a.ncell + icl));
+    R const cflc = (cflo - R(1)) * pra / (pra + Tiny<R>::CFL) + R(1);
+    a.cflo[row] = cflo;
+    a.cflc[row] = cflc;
+    so0n[NEQ - 1] = pra / ga1 + ke + Tiny<R>::CFL;
+    return cflc;
+}
+
+// calc_dsoln for one body cell (euler_gradient.cpp:23-130 with the gradient
+// element of GradientElement.cpp:305-458): per fundamental gradient element
+// solve, W-1/2 weights, W-3/4 cap, weighted sum.  When AB is set the neighbour
+// terms come from soln_cell's alpha/beta; otherwise they are gathered here.
+template <int CT, typename R, typename G, bool AB>
+__device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
+                                           R const * alpha, R const * beta, R * so1n)
+{
+    constexpr int ND = CellT<CT>::ND;
+    constexpr int NEQ = ND + 2;
+    constexpr int NFC = CellT<CT>::NFC;
+    constexpr int NFGE = CellT<CT>::NFGE;
+    using D = Dim<ND>;
+
+    R const acfl = fabs(cflc);
+    R const sgm0 = a.sigma0 / acfl;
+    R const tau = a.taumin + acfl * a.tauscale;
+    R const ofg1 = R(1) / R(NFGE);
+
+    // Gradient-evaluation displacements: idis = dst - delta, dst = P + tau Q.
+    R idis[NFC][ND];
+#pragma unroll
+    for (int f = 0; f < NFC; ++f)
+    {
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            idis[f][d] = fg<ND>(a, f, D::K_P + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl);
+        }
+    }
+    R delta[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        delta[d] = R(0);
+    }
+    if constexpr (!CellT<CT>::SIMPLEX)
+    {
+        // Sub-element centroid of the gradient element about the vertex mean
+        // (calc_gge_centroid, GradientElement.cpp:249-301).
+        R voc = R(0);
+#pragma unroll
+        for (int k = 0; k < NFGE; ++k)
+        {
+            int const f0 = CellT<CT>::fge(k, 0);
+            int const f1 = CellT<CT>::fge(k, 1);
+            int const f2 = (ND == 3) ? CellT<CT>::fge(k, ND - 1) : f1;
+            R const vob = det_rows<ND, R>(idis[f0], idis[f1], idis[f2]);
+            voc += vob;
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                R s = idis[f0][d] + idis[f1][d];
+                if constexpr (ND == 3)
+                {
+                    s += idis[f2][d];
+                }
+                delta[d] += s * vob;
+            }
+        }
+        R const inv = R(1) / (voc * R(ND + 1));
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            delta[d] *= inv;
+        }
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                idis[f][d] -= delta[d];
+            }
+        }
+    }
+
+    // Solution deltas at the evaluation points: uf[f][i].
+    R uf[NFC][NEQ];
+    if constexpr (AB)
+    {
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                uf[f][i] = alpha[f * NEQ + i] - so0n[i] + tau * beta[f * NEQ + i];
+            }
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+            int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
+            R rec[2 * NEQ + NEQ * ND];
+            load_rec<ND, R>(a.cur + jr * D::RS, rec);
+            R jd[ND];
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+            }
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
+#pragma unroll
+                for (int d = 0; d < ND; ++d)
+                {
+                    s += jd[d] * rec[2 * NEQ + i * ND + d];
+                }
+                uf[f][i] = s;
+            }
+        }
+    }
+
+    // Rows of each element's inverse displacement matrix (prescaled by
+    // 1/det): grad = sum_v uf[v] * C[k][v].
+    R C[NFGE][ND][ND];
+#pragma unroll
+    for (int k = 0; k < NFGE; ++k)
+    {
+        R const * ra = idis[CellT<CT>::fge(k, 0)];
+        R const * rb = idis[CellT<CT>::fge(k, 1)];
+        if constexpr (ND == 2)
+        {
+            R const inv = R(1) / (ra[0] * rb[1] - ra[1] * rb[0]);
+            C[k][0][0] = rb[1] * inv;
+            C[k][0][1] = -rb[0] * inv;
+            C[k][1][0] = -ra[1] * inv;
+            C[k][1][1] = ra[0] * inv;
+        }
+        else
+        {
+            R const * rc = idis[CellT<CT>::fge(k, ND - 1)];
+            R const bc0 = rb[1] * rc[2] - rb[2] * rc[1];
+            R const bc1 = rb[2] * rc[0] - rb[0] * rc[2];
+            R const bc2 = rb[0] * rc[1] - rb[1] * rc[0];
+            R const inv = R(1) / (ra[0] * bc0 + ra[1] * bc1 + ra[2] * bc2);
+            C[k][0][0] = bc0 * inv;
+            C[k][0][1] = bc1 * inv;
+            C[k][0][2] = bc2 * inv;
+            C[k][1][0] = (rc[1] * ra[2] - rc[2] * ra[1]) * inv;
+            C[k][1][1] = (rc[2] * ra[0] - rc[0] * ra[2]) * inv;
+            C[k][1][2] = (rc[0] * ra[1] - rc[1] * ra[0]) * inv;
+            C[k][2][0] = (ra[1] * rb[2] - ra[2] * rb[1]) * inv;
+            C[k][2][1] = (ra[2] * rb[0] - ra[0] * rb[2]) * inv;
+            C[k][2][2] = (ra[0] * rb[1] - ra[1] * rb[0]) * inv;
+        }
+    }
+
+    uint8_t fired = 0;
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        R grad[NFGE][ND];
+        R wgt[NFGE];
+        R wacc = R(0);
+#pragma unroll
+        for (int k = 0; k < NFGE; ++k)
+        {
+            R sq = R(0);
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                R s = R(0);
+#pragma unroll
+                for (int v = 0; v < ND; ++v)
+                {
+                    s += uf[CellT<CT>::fge(k, v)][i] * C[k][v][d];
+                }
+                grad[k][d] = s;
+                sq += s * s;
+            }
+            // W-1/2 weighting: inverse gradient magnitude.
+            wgt[k] = rsq(sq + Tiny<R>::AZ);
+            wacc += wgt[k];
+        }
+        R const rw = R(1) / wacc;
+        R wmax = R(0);
+        R wmin = R(0);
+#pragma unroll
+        for (int k = 0; k < NFGE; ++k)
+        {
+            wgt[k] = wgt[k] * rw - ofg1;
+            wmax = fmax(wmax, wgt[k]);
+            wmin = fmin(wmin, wgt[k]);
+        }
+        // W-3/4 cap.
+        R const sm = fmin((R(1) - ofg1) / (wmax + Tiny<R>::AZ), -ofg1 / (wmin - Tiny<R>::AZ));
+        R const sig = fmin(sm, sgm0);
+        if (sm < sgm0)
+        {
+            fired |= static_cast<uint8_t>(1u << i);
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            R s = R(0);
+#pragma unroll
+            for (int k = 0; k < NFGE; ++k)
+            {
+                s += (ofg1 + sig * wgt[k]) * grad[k][d];
+            }
+            so1n[i * ND + d] = s;
+        }
+    }
+    if (a.limiter)
+    {
+        a.limiter[icl] = fired;
+    }
+}
+
+// Ghost-row order-0 update of one boundary face (euler_bc.cpp:147-215):
+// ghost so0n from the interior's so0n (taken before calc_cfl's rewrite).
+template <int ND, typename R>
+__device__ __forceinline__ void bc0_ghost(int kind, double const * n, double const * val, R const * in, R * out)
+{
+    constexpr int NEQ = ND + 2;
+    if (kind == 2)
+    {
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i)
+        {
+            out[i] = R(val[i]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        out[i] = in[i];
+    }
+    if (kind == 1)
+    {
+        // Reflect the momentum: m - 2 (m . n) n.
+        R mn = R(0);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            mn += in[1 + d] * R(n[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            out[1 + d] = in[1 + d] - R(2) * mn * R(n[d]);
+        }
+    }
+}
+
+// Ghost-row order-1 update of one boundary face (euler_bc.cpp:221-320):
+// ghost so1n from the interior's so1c.
+template <int ND, typename R>
+__device__ __forceinline__ void bc1_ghost(int kind, double const * n, R const * g, R * out)
+{
+    constexpr int NEQ = ND + 2;
+    if (kind == 2)
+    {
+#pragma unroll
+        for (int i = 0; i < NEQ * ND; ++i)
+        {
+            out[i] = R(0);
+        }
+        return;
+    }
+    R nn[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        nn[d] = R(n[d]);
+    }
+    if (kind == 0)
+    {
+        // Tangential projection of every gradient: g - (g . n) n.
+#pragma unroll
+        for (int i = 0; i < NEQ; ++i)
+        {
+            R gn = R(0);
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                gn += g[i * ND + d] * nn[d];
+            }
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                out[i * ND + d] = g[i * ND + d] - gn * nn[d];
+            }
+        }
+        return;
+    }
+    // Slip wall: scalar gradients reflected (I - 2 n n^T) g; momentum
+    // gradient tensor reflected on both indices, R G R.
+#pragma unroll
+    for (int ii = 0; ii < 2; ++ii)
+    {
+        int const i = ii == 0 ? 0 : NEQ - 1;
+        R gn = R(0);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            gn += g[i * ND + d] * nn[d];
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            out[i * ND + d] = g[i * ND + d] - R(2) * gn * nn[d];
+        }
+    }
+    // RG = G - 2 (G n) n^T then R(RG) = RG - 2 n (n^T RG).
+    R gm[ND][ND];
+#pragma unroll
+    for (int p = 0; p < ND; ++p)
+    {
+        R gnp = R(0);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            gnp += g[(1 + p) * ND + d] * nn[d];
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            gm[p][d] = g[(1 + p) * ND + d] - R(2) * gnp * nn[d];
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        R ntg = R(0);
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+        {
+            ntg += nn[p] * gm[p][d];
+        }
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+        {
+            out[(1 + p) * ND + d] = gm[p][d] - R(2) * nn[p] * ntg;
+        }
+    }
+}
+
+// One fused CESE substep for one body cell: soln, bc_soln of its boundary
+// faces, cfl, dsoln, bc_dsoln of its boundary faces, and calc_solt of the next
+// substep for its own row and its ghost rows.  Reads only the current records
+// (neighbours' old values) and writes only rows it owns, so one launch covers
+// the whole substep with no grid-wide synchronisation.
+template <int CT, typename R, typename G>
+__device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t icl)
+{
+    constexpr int ND = CellT<CT>::ND;
+    constexpr int NEQ = ND + 2;
+    constexpr int NFC = CellT<CT>::NFC;
+    constexpr bool AB = CellT<CT>::SIMPLEX;
+    using D = Dim<ND>;
+    int64_t const row = icl + a.ngst;
+
+    R so0n[NEQ];
+    R alpha[AB ? NFC * NEQ : 1];
+    R beta[AB ? NFC * NEQ : 1];
+    soln_cell<CT, R, G, AB>(a, icl, so0n, alpha, beta);
+
+    // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
+#pragma unroll
+    for (int f = 0; f < NFC; ++f)
+    {
+        int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
+        if (jr < a.ngst)
+        {
+            int const kind = a.gkind[jr];
+            if (kind >= 0)
+            {
+                R own[2 * NEQ + NEQ * ND];
+                load_rec<ND, R>(a.cur + row * D::RS, own);
+                R g0[NEQ], g1[NEQ * ND], gt[NEQ];
+                bc0_ghost<ND, R>(kind, a.gnml + jr * ND, a.gval + jr * NEQ, so0n, g0);
+                bc1_ghost<ND, R>(kind, a.gnml + jr * ND, own + 2 * NEQ, g1);
+                solt_row<ND, R>(g0, g1, ldg(a.gamma + jr), gt);
+                store_rec<ND, R>(a.nxt + jr * D::RS, g0, gt, g1);
+            }
+        }
+    }
+
+    R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n);
+    R so1n[NEQ * ND];
+    dsoln_cell<CT, R, G, AB>(a, icl, so0n, cflc, alpha, beta, so1n);
+    R so0t[NEQ];
+    solt_row<ND, R>(so0n, so1n, ldg(a.gamma + row), so0t);
+    store_rec<ND, R>(a.nxt + row * D::RS, so0n, so0t, so1n);
+}
+
+template <int ND, typename R, typename G>
+__global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
+{
+    int64_t const t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t < a.ncell)
+    {
+        int const ct = a.ctype[t];
+        if constexpr (ND == 2)
+        {
+            if (ct == 4)
+                fused_cell<4, R, G>(a, t);
+            else
+                fused_cell<3, R, G>(a, t);
+        }
+        else
+        {
+            switch (ct)
+            {
+            case 6: fused_cell<6, R, G>(a, t); break;
+            case 5: fused_cell<5, R, G>(a, t); break;
+            case 7: fused_cell<7, R, G>(a, t); break;
+            default: fused_cell<8, R, G>(a, t); break;
+            }
+        }
+    }
+    else if (t < a.ncell + a.ngst)
+    {
+        // A ghost row without a boundary condition keeps its stale state; its
+        // next so0t is still the Jacobian product of that state.
+        int64_t const g = t - a.ncell;
+        if (a.gkind[g] < 0)
+        {
+            constexpr int NEQ = ND + 2;
+            R rec[2 * NEQ + NEQ * ND];
+            load_rec<ND, R>(a.nxt + g * Dim<ND>::RS, rec);
+            R tt[NEQ];
+            solt_row<ND, R>(rec, rec + 2 * NEQ, ldg(a.gamma + g), tt);
+            store_rec<ND, R>(a.nxt + g * Dim<ND>::RS, rec, tt, rec + 2 * NEQ);
+        }
+    }
+}
+
+} // namespace dev
+} // namespace scg

@@ -1,0 +1,166 @@
+"""Unstructured mixed-element mesh with a mirrored ghost layer.
+
+Mirrors solvcon's ``StaticMesh`` Python surface
+(cpp/solvcon/mesh/pymod/wrap_StaticMesh.cpp:61-181): the constructor
+``StaticMesh(ndim, nnode, nface=0, ncell=0)``, the cell-type constants, the
+size properties, ``build_interior``/``build_boundary``/``build_ghost``/
+``build_edge``, ``add_bc``/``bc``/``bcs`` and the fifteen table properties as
+ghost-aware :class:`~solvcon_gb300.buffer.SimpleArray` views.  The tables live
+in the native library (host memory) and the views alias them.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib, ptr
+from .buffer import SimpleArray
+
+__all__ = ["StaticMesh", "StaticMeshBc"]
+
+_ARRAYS = ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol", "fctpn",
+           "cltpn", "clgrp", "fcnds", "fccls", "clnds", "clfcs", "ednds",
+           "bndfcs")
+
+
+class StaticMeshBc:
+    """A boundary group of a :class:`StaticMesh` (StaticMesh.hpp:159-251)."""
+
+    def __init__(self, name, facn):
+        self.name = name
+        self.facn = facn
+
+    @property
+    def nbound(self):
+        return self.facn.shape[0]
+
+
+class StaticMesh:
+    """Mixed-element unstructured mesh (StaticMesh.hpp:264-456)."""
+
+    NONCELLTYPE = 0
+    POINT = 1
+    LINE = 2
+    QUADRILATERAL = 3
+    TRIANGLE = 4
+    HEXAHEDRON = 5
+    TETRAHEDRON = 6
+    PRISM = 7
+    PYRAMID = 8
+
+    FCMND = 4
+    CLMND = 8
+    CLMFC = 6
+    FCREL = 4
+    BFREL = 3
+
+    def __init__(self, ndim, nnode, nface=0, ncell=0):
+        h = ctypes.c_void_p()
+        check(lib.scg_mesh_create(int(ndim), int(nnode), int(nface),
+                                  int(ncell), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib.scg_mesh_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        """The native scg_mesh handle (for the C ABI)."""
+        return self._h
+
+    # -- sizes --------------------------------------------------------------
+
+    def _sizes(self):
+        out = np.zeros(10, dtype="int64")
+        check(lib.scg_mesh_sizes(self._h, ptr(out)))
+        return out
+
+    ndim = property(lambda self: int(self._sizes()[0]))
+    nnode = property(lambda self: int(self._sizes()[1]))
+    nface = property(lambda self: int(self._sizes()[2]))
+    ncell = property(lambda self: int(self._sizes()[3]))
+    nbound = property(lambda self: int(self._sizes()[4]))
+    ngstnode = property(lambda self: int(self._sizes()[5]))
+    ngstface = property(lambda self: int(self._sizes()[6]))
+    ngstcell = property(lambda self: int(self._sizes()[7]))
+    nedge = property(lambda self: int(self._sizes()[8]))
+    nbcs = property(lambda self: int(self._sizes()[9]))
+
+    # -- builds -------------------------------------------------------------
+
+    def build_interior(self, do_metric=True, build_edge=True):
+        check(lib.scg_mesh_build_interior(self._h, int(bool(do_metric)),
+                                          int(bool(build_edge))))
+
+    def build_edge(self):
+        check(lib.scg_mesh_build_edge(self._h))
+
+    def build_boundary(self):
+        check(lib.scg_mesh_build_boundary(self._h))
+
+    def build_ghost(self):
+        check(lib.scg_mesh_build_ghost(self._h))
+
+    def add_bc(self, name, faces):
+        f = np.ascontiguousarray(faces, dtype="int32")
+        check(lib.scg_mesh_add_bc(self._h, name.encode(), ptr(f), f.size))
+        return self.bc(self.nbcs - 1)
+
+    def bc(self, key):
+        if isinstance(key, str):
+            for b in self.bcs:
+                if b.name == key:
+                    return b
+            raise KeyError(key)
+        buf = ctypes.create_string_buffer(256)
+        nb = ctypes.c_int64()
+        check(lib.scg_mesh_bc(self._h, int(key), buf, 256, None,
+                              ctypes.byref(nb)))
+        facn = np.zeros((nb.value, 3), dtype="int32")
+        check(lib.scg_mesh_bc(self._h, int(key), buf, 256, ptr(facn),
+                              ctypes.byref(nb)))
+        return StaticMeshBc(buf.value.decode(), facn)
+
+    @property
+    def bcs(self):
+        return [self.bc(i) for i in range(self.nbcs)]
+
+    # -- tables -------------------------------------------------------------
+
+    def _table(self, which):
+        data = ctypes.c_void_p()
+        shape = np.zeros(3, dtype="int64")
+        nd = ctypes.c_int()
+        ngh = ctypes.c_int64()
+        dt = ctypes.c_int()
+        check(lib.scg_mesh_array(self._h, which, ctypes.byref(data),
+                                 ptr(shape), ctypes.byref(nd),
+                                 ctypes.byref(ngh), ctypes.byref(dt)))
+        ctype = ctypes.c_double if dt.value == 0 else ctypes.c_int32
+        dtype = "float64" if dt.value == 0 else "int32"
+        n = int(shape[0] * shape[1])
+        shp = (int(shape[0]), int(shape[1])) if nd.value == 2 else \
+            (int(shape[0]),)
+        if n == 0 or not data.value:
+            return np.zeros(shp, dtype=dtype), int(ngh.value)
+        raw = (ctype * n).from_address(data.value)
+        raw._owner = self  # keep the mesh (and its buffers) alive
+        return np.frombuffer(raw, dtype=dtype).reshape(shp), int(ngh.value)
+
+    def _view(self, which):
+        return SimpleArray(lambda: self._table(which)[0],
+                           nghost=self._table(which)[1])
+
+
+def _make_prop(i):
+    return property(lambda self: self._view(i))
+
+
+for _i, _name in enumerate(_ARRAYS):
+    setattr(StaticMesh, _name, _make_prop(_i))
+del _i, _name, _make_prop
+_ = _lib
