@@ -17,7 +17,7 @@ import numpy as np
 
 from .mesh import StaticMesh
 
-__all__ = ["tri_square", "tet_cube", "quad_square", "build_mesh",
+__all__ = ["tri_square", "tet_cube", "quad_square", "hex_cube", "prism_slab", "build_mesh",
            "quadrant_state", "blast_state", "conserved", "set_state"]
 
 
@@ -106,6 +106,48 @@ def tet_cube(nside, jitter=0.15, seed=0):
     clnds[:, 0] = 4
     clnds[:, 1:5] = tets
     cltpn = np.full(tets.shape[0], StaticMesh.TETRAHEDRON, dtype="int32")
+    return ndcrd, cltpn, clnds
+
+
+def hex_cube(nside, jitter=0.0, seed=0):
+    """(Jittered) hexahedral unit cube: (ndcrd, cltpn, clnds)."""
+    n = int(nside)
+    xs = np.linspace(0.0, 1.0, n + 1)
+    gz, gy, gx = np.meshgrid(xs, xs, xs, indexing="ij")
+    ndcrd = np.stack([gx.ravel(), gy.ravel(), gz.ravel()], axis=1)
+    if jitter:
+        ndcrd = _jitter(ndcrd, n, 3, jitter, seed)
+    k, j, i = np.meshgrid(np.arange(n), np.arange(n), np.arange(n),
+                          indexing="ij")
+    s = n + 1
+    base = (k * s * s + j * s + i).ravel()
+    off = np.array([0, 1, 1 + s, s, s * s, 1 + s * s, 1 + s + s * s,
+                    s + s * s], dtype="int64")
+    clnds = np.full((base.size, 9), -1, dtype="int32")
+    clnds[:, 0] = 8
+    clnds[:, 1:9] = base[:, None] + off[None, :]
+    cltpn = np.full(base.size, StaticMesh.HEXAHEDRON, dtype="int32")
+    return ndcrd, cltpn, clnds
+
+
+def prism_slab(nside, nz, jitter=0.0, seed=0):
+    """Triangulated unit square (:func:`tri_square`) extruded into nz layers
+    of prisms over z in [0, 1]: (ndcrd, cltpn, clnds)."""
+    x2, _, c2 = tri_square(nside, jitter, seed)
+    nn = x2.shape[0]
+    zs = np.linspace(0.0, 1.0, nz + 1)
+    ndcrd = np.concatenate([np.column_stack([x2, np.full(nn, z)])
+                            for z in zs])
+    tri = c2[:, 1:4].astype("int64")
+    cells = []
+    for layer in range(nz):
+        lo = tri + layer * nn
+        cells.append(np.concatenate([lo, lo + nn], axis=1))
+    pr = np.concatenate(cells)
+    clnds = np.full((pr.shape[0], 9), -1, dtype="int32")
+    clnds[:, 0] = 6
+    clnds[:, 1:7] = pr
+    cltpn = np.full(pr.shape[0], StaticMesh.PRISM, dtype="int32")
     return ndcrd, cltpn, clnds
 
 

@@ -1,0 +1,140 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference solvcon implementation (oracle/_ref/libsolvcon_ref.so,
+built from the reference's own sources by ``make -C oracle ref``) on small
+seeded cases and stores its outputs as .npz files:
+
+* mesh_<case>.npz -- every StaticMesh table after build_interior,
+  build_boundary and build_ghost (the mesh builder's golden vectors);
+* march_<case>.npz -- initial state, boundary setup and the EulerCore arrays
+  after a number of march steps (the march's golden vectors);
+* e1d_sod.npz -- the Euler1DCore Sod tube after march_alpha2.
+
+Usage: python tests/golden/make_golden.py   (needs oracle/_ref built)
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refbind as rb  # noqa: E402
+from solvcon_gb300 import meshgen  # noqa: E402
+
+MESH_ARRAYS = ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol", "fctpn",
+               "cltpn", "fcnds", "fccls", "clnds", "clfcs", "ednds", "bndfcs")
+
+
+def fixture_cases():
+    """Hand-built fixture meshes of the reference tests
+    (tests/test_multidim.py:152-281, 810-827) plus seeded jittered meshes."""
+    cases = {
+        "tri3": (2, [(0, 0), (-1, -1), (1, -1), (0, 1)], [4, 4, 4],
+                 [(3, 0, 1, 2), (3, 0, 2, 3), (3, 0, 3, 1)]),
+        "quad1": (2, [(0, 0), (1, 0), (1, 1), (0, 1)], [3],
+                  [(4, 0, 1, 2, 3)]),
+        "mixed": (2, [(0, 0), (1, 0), (2, 0), (0, 1), (1, 1), (2, 1)],
+                  [3, 4, 4], [(4, 0, 1, 4, 3), (3, 1, 2, 4, 0),
+                              (3, 2, 5, 4, 0)]),
+        "tet1": (3, [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)], [6],
+                 [(4, 0, 1, 2, 3)]),
+        "hex1": (3, [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1),
+                     (1, 0, 1), (1, 1, 1), (0, 1, 1)], [5],
+                 [(8, 0, 1, 2, 3, 4, 5, 6, 7)]),
+        "prism1": (3, [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1),
+                       (1, 0, 1), (0, 1, 1)], [7], [(6, 0, 1, 2, 3, 4, 5)]),
+        "pyr1": (3, [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0),
+                     (0.5, 0.5, 1)], [8], [(5, 0, 1, 2, 3, 4)]),
+    }
+    x, t, c = meshgen.tri_square(12, 0.2, seed=11)
+    cases["tri12"] = (2, x, t, c[:, :4])
+    x, t, c = meshgen.quad_square(8, 0.15, seed=12)
+    cases["quad8"] = (2, x, t, c[:, :5])
+    x, t, c = meshgen.tet_cube(3, 0.15, seed=13)
+    cases["tet3"] = (3, x, t, c[:, :5])
+    return cases
+
+
+def mesh_golden(name, nd, x, t, c):
+    r = rb.RefMesh(nd, x, t, c)
+    out = {"ndim": nd, "ndcrd_in": np.asarray(x, dtype="float64"),
+           "cltpn_in": np.asarray(t, dtype="int32"),
+           "clnds_in": np.asarray(c, dtype="int32")}
+    sizes = r.sizes()
+    out["sizes"] = np.array([sizes[k] for k in
+                             ("ndim", "nnode", "nface", "ncell", "nbound",
+                              "ngstnode", "ngstface", "ngstcell", "nedge",
+                              "nbcs")], dtype="int64")
+    for a in MESH_ARRAYS:
+        out[a] = r.array(a)
+    np.savez_compressed(os.path.join(HERE, "mesh_%s.npz" % name), **out)
+    return r
+
+
+def march_golden(name, mesh, nd, state, bc_kind, dt, steps):
+    e = rb.RefEuler(mesh, dt)
+    e.init_solution(1.4, 1.0, [0.0] * nd, 1.0)
+    ng = mesh.sizes()["ngstcell"]
+    so = e.get("so0n")
+    so[ng:] = state
+    e.set("so0n", so)
+    faces = mesh.array("bndfcs").reshape(-1, 3)[:, 0]
+    e.add_bc(bc_kind, faces)
+    e.call("bc_soln")
+    e.call("bc_dsoln")
+    out = {"dt": dt, "steps": steps, "bc_kind": bc_kind,
+           "state0": np.asarray(state), "faces": faces}
+    e.march(steps)
+    for a in ("cevol", "cecnd", "so0c", "so0n", "so0t", "so1c", "so1n",
+              "cflo", "cflc"):
+        out[a] = e.get(a)
+    np.savez_compressed(os.path.join(HERE, "march_%s.npz" % name), **out)
+
+
+def e1d_golden():
+    # Sod tube of the 1D configuration: 201 points on [-1, 1],
+    # dt = 2 * 0.8 * dx / 2.19 (post-shock max |u| + c), 28 steps.
+    n = 201
+    dx = 2.0 / (n - 1)
+    dt = 2 * 0.8 * dx / 2.19
+    c = rb.RefEuler1D(n, dt)
+    x = np.linspace(-1, 1, n)
+    c.set("coord", x)
+    g = 1.4
+    so0 = np.zeros((n, 3))
+    left = x < 0.0
+    so0[:, 0] = np.where(left, 1.0, 0.125)
+    so0[:, 2] = np.where(left, 1.0 / (g - 1), 0.1 / (g - 1))
+    c.set("so0", so0)
+    c.set("so1", np.zeros((n, 3)))
+    c.set("gamma", np.full(n, g))
+    c.set("cfl", np.zeros(n))
+    c.setup_march()
+    out = {"dt": dt, "steps": 28, "coord": x, "so0_in": so0}
+    c.march_alpha(2, 28)
+    for a in ("so0", "so1", "cfl"):
+        out[a] = c.get(a)
+    np.savez_compressed(os.path.join(HERE, "e1d_sod.npz"), **out)
+
+
+def main():
+    cases = fixture_cases()
+    meshes = {k: mesh_golden(k, *v) for k, v in cases.items()}
+    for name, kind in (("tri12", 1), ("quad8", 0), ("tet3", 1)):
+        mesh = meshes[name]
+        nd = cases[name][0]
+        clcnd = mesh.array("clcnd").reshape(-1, nd)[mesh.sizes()["ngstcell"]:]
+        state = meshgen.quadrant_state(clcnd[:, :2], seed=5) if nd == 2 \
+            else meshgen.blast_state(clcnd, center=(0.5, 0.5, 0.5),
+                                     radius=0.35)
+        march_golden(name, mesh, nd, state, kind, 2e-3, 6)
+    e1d_golden()
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

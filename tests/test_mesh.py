@@ -1,0 +1,125 @@
+"""Host mesh builder parity: the StaticMesh tables equal the reference's.
+
+Golden vectors come from the reference itself (tests/golden/make_golden.py);
+where the reference library is built here (oracle/_ref) the same checks run
+against it directly on extra seeded meshes.
+"""
+
+import numpy as np
+import pytest
+
+from _util import golden
+
+CASES = ("tri3", "quad1", "mixed", "tet1", "hex1", "prism1", "pyr1", "tri12",
+         "quad8", "tet3")
+INT_ARRAYS = ("fctpn", "cltpn", "fcnds", "fccls", "clfcs", "ednds", "bndfcs")
+REAL_ARRAYS = ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol")
+SIZES = ("ndim", "nnode", "nface", "ncell", "nbound", "ngstnode", "ngstface",
+         "ngstcell", "nedge", "nbcs")
+
+
+def _build(g):
+    from solvcon_gb300 import StaticMesh
+    nd = int(g["ndim"])
+    x, t, c = g["ndcrd_in"], g["cltpn_in"], g["clnds_in"]
+    m = StaticMesh(ndim=nd, nnode=len(x), nface=0, ncell=len(t))
+    m.ndcrd[:, :] = x
+    m.cltpn[:] = t
+    m.clnds[:, :c.shape[1]] = c
+    m.build_interior(do_metric=True, build_edge=True)
+    m.build_boundary()
+    m.build_ghost()
+    return m
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mesh_matches_reference_golden(case):
+    g = golden("mesh_" + case)
+    m = _build(g)
+    assert [getattr(m, k) for k in SIZES] == list(g["sizes"])
+    for name in INT_ARRAYS:
+        got = np.asarray(getattr(m, name).ndarray).ravel()
+        assert np.array_equal(got, g[name]), name
+    # clnds: the reference leaves unused columns uninitialised; compare the
+    # node counts and node lists only.
+    got = np.asarray(m.clnds.ndarray)
+    want = g["clnds"].reshape(got.shape)
+    for row in range(got.shape[0]):
+        n = want[row, 0]
+        assert np.array_equal(got[row, :n + 1], want[row, :n + 1])
+    for name in REAL_ARRAYS:
+        got = np.asarray(getattr(m, name).ndarray).ravel()
+        np.testing.assert_allclose(got, g[name], rtol=1e-14, atol=1e-15,
+                                   err_msg=name)
+
+
+def test_ghost_indexing_and_views():
+    from _util import fixture_mesh
+    m = fixture_mesh("tri3")
+    assert m.ngstcell == 3 and m.clcnd.nghost == 3
+    full = np.asarray(m.clcnd.ndarray)
+    assert m.clcnd[-1, 0] == full[2, 0]
+    assert m.clcnd[0, 1] == full[3, 1]
+    with pytest.raises(IndexError):
+        m.clcnd[-4, 0]
+    with pytest.raises(IndexError):
+        m.clcnd[3, 0]
+    # A view taken before a rebuild keeps its old buffer alive.
+    assert m.fccls[0, 0] >= 0
+
+
+def test_add_bc_validation():
+    from solvcon_gb300 import StaticMesh
+    m = StaticMesh(ndim=2, nnode=4, nface=0, ncell=1)
+    m.ndcrd[:, :] = [(0, 0), (1, 0), (1, 1), (0, 1)]
+    m.cltpn[:] = [StaticMesh.QUADRILATERAL]
+    m.clnds[:, :5] = [(4, 0, 1, 2, 3)]
+    m.build_interior()
+    with pytest.raises(ValueError):
+        m.add_bc("", [0])
+    with pytest.raises(ValueError):
+        m.add_bc("x", [99])
+    b = m.add_bc("left", [3])
+    assert b.name == "left"
+    with pytest.raises(ValueError):
+        m.add_bc("left", [2])
+    with pytest.raises(ValueError):
+        m.add_bc("again", [3])
+    m.build_boundary()
+    assert m.nbound == 4 and m.nbcs == 2
+    assert m.bc("left").facn[0, 0] == 3
+    assert [b.name for b in m.bcs] == ["left", "<NONAME>"]
+    with pytest.raises(RuntimeError):
+        m.build_boundary()
+
+
+def test_bad_inputs_raise():
+    from solvcon_gb300 import StaticMesh
+    with pytest.raises(ValueError):
+        StaticMesh(ndim=4, nnode=1, nface=0, ncell=1)
+    m = StaticMesh(ndim=2, nnode=3, nface=0, ncell=1)
+    m.cltpn[:] = [StaticMesh.TRIANGLE]
+    m.clnds[:, :4] = [(3, 0, 1, 7)]
+    with pytest.raises(IndexError):
+        m.build_interior()
+
+
+def _ref():
+    from oracle import refbind
+    if not refbind.available():
+        pytest.skip("reference library not built on this host")
+    return refbind
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_mesh_matches_reference_library(seed):
+    rb = _ref()
+    from solvcon_gb300 import meshgen
+    for nd, (x, t, c) in ((2, meshgen.tri_square(9, 0.2, seed)),
+                          (3, meshgen.tet_cube(3, 0.15, seed))):
+        m = meshgen.build_mesh(nd, x, t, c)
+        r = rb.RefMesh(nd, x, t, c[:, :5])
+        m.build_edge()
+        for name in INT_ARRAYS + REAL_ARRAYS:
+            got = np.asarray(getattr(m, name).ndarray).ravel()
+            assert np.array_equal(got, r.array(name)), name

@@ -1,0 +1,465 @@
+"""GPU EulerCore: behaviour of the reference's EulerCore tests and parity
+with the oracle, per operation and over multi-step marches.
+
+Modelled on the reference's tests/test_multidim.py (solution storage, CFL,
+flux homogeneity, free stream, linear-field gradient recovery, boundary
+conditions, bounded channel march), with the CPU oracle (a bit-exact
+restatement of the reference, pinned in test_oracle.py) as the checker.
+
+Tolerances (FP64): one operation on the same inputs agrees with the oracle to
+1e-12 relative to the largest magnitude of the compared array (the GPU
+evaluates the same mathematics in a different operation order); marches of a
+few steps agree to 1e-10.
+"""
+
+import numpy as np
+import pytest
+
+from _util import FIXTURES, assert_rel, fixture_mesh, quad_channel
+
+pytestmark = pytest.mark.gpu
+
+GAMMA, RHO, PRES = 1.4, 1.2, 0.9
+VEL = (0.3, -0.15, 0.05)
+
+
+def _core(mesh, dt=0.01, precision="fp64"):
+    import solvcon_gb300 as sg
+    return sg.EulerCore(mesh=mesh, time_increment=dt, precision=precision)
+
+
+def _uniform_row(nd):
+    v = VEL[:nd]
+    e = PRES / (GAMMA - 1.0) + 0.5 * RHO * sum(c * c for c in v)
+    return [RHO] + [RHO * c for c in v] + [e]
+
+
+def _flux(u, gamma):
+    nd = u.size - 2
+    rho, mom, en = u[0], u[1:1 + nd], u[nd + 1]
+    vel = mom / rho
+    p = (gamma - 1.0) * (en - 0.5 * rho * vel @ vel)
+    f = np.zeros((u.size, nd))
+    for d in range(nd):
+        f[0, d] = mom[d]
+        for k in range(nd):
+            f[1 + k, d] = mom[k] * vel[d] + (p if k == d else 0.0)
+        f[nd + 1, d] = (en + p) * vel[d]
+    return f
+
+
+# -- solution storage and initialisation (test_multidim.py:394-600) ---------
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_storage_and_init(name):
+    mesh = fixture_mesh(name)
+    ec = _core(mesh)
+    nd, neq = mesh.ndim, mesh.ndim + 2
+    tot = ec.ngstcell + ec.ncell
+    assert ec.neq == neq
+    for a in ("so0c", "so0n", "so0t", "stm"):
+        assert getattr(ec, a).shape == (tot, neq)
+    for a in ("so1c", "so1n"):
+        assert getattr(ec, a).shape == (tot, neq, nd)
+    for a in ("cflo", "cflc", "gamma"):
+        assert getattr(ec, a).shape == (tot,)
+    ec.init_solution(gamma=GAMMA, rho=RHO, v=list(VEL[:nd]), p=PRES)
+    row = _uniform_row(nd)
+    for icl in range(ec.ncell):
+        np.testing.assert_allclose([ec.so0n[icl, k] for k in range(neq)], row)
+    for icl in range(-ec.ngstcell, 0):
+        assert all(ec.so0n[icl, k] == 0.0 for k in range(neq))
+    np.testing.assert_allclose(ec.gamma.ndarray, GAMMA)
+    for bad in (dict(v=[0.1] * (nd - 1)), dict(gamma=1.0), dict(rho=0.0),
+                dict(p=-1.0)):
+        args = dict(gamma=GAMMA, rho=RHO, v=list(VEL[:nd]), p=PRES)
+        args.update(bad)
+        with pytest.raises(ValueError):
+            ec.init_solution(**args)
+    assert ec.sigma0 == 3.0 and ec.taumin == 0.0 and ec.tauscale == 1.0
+    ec.sigma0, ec.taumin, ec.tauscale = 2.5, 0.1, 0.7
+    assert (ec.sigma0, ec.taumin, ec.tauscale) == (2.5, 0.1, 0.7)
+
+
+@pytest.mark.parametrize("name", ["tri3", "mixed", "tet1", "hex1"])
+def test_calc_cfl_uniform_and_negative_pressure(name):
+    mesh = fixture_mesh(name)
+    ec = _core(mesh)
+    nd = mesh.ndim
+    v = VEL[:nd]
+    ec.init_solution(gamma=GAMMA, rho=RHO, v=list(v), p=PRES)
+    ec.calc_cfl()
+    hdt = ec.time_increment / 2.0
+    wspd = np.sqrt(GAMMA * PRES / RHO) + np.sqrt(sum(c * c for c in v))
+    cecnd = ec.cecnd
+    for icl in range(ec.ncell):
+        nfc = mesh.clfcs[icl, 0]
+        dist = min(np.sqrt(sum((cecnd[icl, f * nd + d] - cecnd[icl, d]) ** 2
+                               for d in range(nd))) for f in range(1, nfc + 1))
+        np.testing.assert_allclose(ec.cflo[icl], hdt * wspd / dist, rtol=1e-13)
+        np.testing.assert_allclose(ec.cflc[icl], ec.cflo[icl], rtol=1e-13)
+    for icl in range(ec.ncell):
+        ec.so0n[icl, nd + 1] = 0.0
+    ec.calc_cfl()
+    ke = sum((RHO * c) ** 2 for c in v) / (2.0 * RHO)
+    for icl in range(ec.ncell):
+        np.testing.assert_allclose(ec.cflc[icl], 1.0, rtol=1e-14)
+        np.testing.assert_allclose(ec.so0n[icl, nd + 1], ke, rtol=1e-13)
+
+
+def test_update_swaps_buffers():
+    ec = _core(fixture_mesh("mixed"))
+    ec.init_solution(gamma=GAMMA, rho=RHO, v=[0.3, -0.15], p=PRES)
+    view = ec.so1n.ndarray
+    view[...] = np.arange(view.size, dtype="float64").reshape(view.shape)
+    before = {a: np.array(getattr(ec, a).ndarray)
+              for a in ("so0c", "so0n", "so1c", "so1n")}
+    ec.update()
+    np.testing.assert_array_equal(ec.so0c.ndarray, before["so0n"])
+    np.testing.assert_array_equal(ec.so0n.ndarray, before["so0c"])
+    np.testing.assert_array_equal(ec.so1c.ndarray, before["so1n"])
+    np.testing.assert_array_equal(ec.so1n.ndarray, before["so1c"])
+    # The view taken before update() still aliases the same table.
+    np.testing.assert_array_equal(view, ec.so1c.ndarray)
+
+
+# -- marching primitives (test_multidim.py:632-770) -------------------------
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_calc_solt_is_minus_flux_combination(name):
+    mesh = fixture_mesh(name)
+    ec = _core(mesh)
+    nd, neq = mesh.ndim, mesh.ndim + 2
+    row = np.array(_uniform_row(nd))
+    coef = np.array([0.7, -1.3, 0.4][:nd])
+    so0c, so1c, gamma = (np.array(ec.so0c.ndarray), np.array(ec.so1c.ndarray),
+                         np.array(ec.gamma.ndarray))
+    ng = ec.ngstcell
+    gamma[ng:] = GAMMA
+    so0c[ng:] = row
+    so1c[ng:] = row[None, :, None] * coef[None, None, :]
+    ec.gamma.ndarray[...] = gamma
+    ec.so0c.ndarray[...] = so0c
+    ec.so1c.ndarray[...] = so1c
+    ec.calc_solt()
+    expect = -(_flux(row, GAMMA) * coef[None, :]).sum(axis=1)
+    got = np.array(ec.so0t.ndarray)[ng:]
+    np.testing.assert_allclose(got, np.broadcast_to(expect, got.shape),
+                               rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_calc_soln_preserves_free_stream(name):
+    mesh = fixture_mesh(name)
+    ec = _core(mesh)
+    row = _uniform_row(mesh.ndim)
+    ec.gamma.ndarray[...] = GAMMA
+    ec.so0c.ndarray[...] = row
+    ec.so0t.ndarray[...] = 0.0
+    ec.so1c.ndarray[...] = 0.0
+    ec.calc_solt()
+    ec.calc_soln()
+    got = np.array(ec.so0n.ndarray)[ec.ngstcell:]
+    np.testing.assert_allclose(got, np.broadcast_to(row, got.shape),
+                               rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_calc_dsoln_recovers_linear_field(name):
+    mesh = fixture_mesh(name)
+    ec = _core(mesh)
+    nd, neq = mesh.ndim, mesh.ndim + 2
+    g = np.array([[0.1 * (i + 1) + 0.01 * (d + 1) for d in range(nd)]
+                  for i in range(neq)])
+    c = np.array([0.5 + 0.3 * i for i in range(neq)])
+    cecnd = np.array(ec.cecnd.ndarray)
+    clcnd = np.array(mesh.clcnd.ndarray)
+    ng = ec.ngstcell
+    pts = np.where(np.arange(-ng, ec.ncell)[:, None] >= 0, cecnd[:, :nd],
+                   clcnd)
+    vals = c[None, :] + pts @ g.T
+    ec.so0c.ndarray[...] = vals
+    ec.so0n.ndarray[...] = vals
+    ec.so0t.ndarray[...] = 0.0
+    ec.so1c.ndarray[...] = g[None]
+    ec.cflc.ndarray[...] = 0.5
+    ec.calc_dsoln()
+    got = np.array(ec.so1n.ndarray)[ng:]
+    np.testing.assert_allclose(got, np.broadcast_to(g, got.shape), rtol=1e-9,
+                               atol=1e-10)
+
+
+# -- boundary conditions (test_multidim.py:810-1084) ------------------------
+
+def _bnd(mesh):
+    faces = [int(f) for f in mesh.bndfcs.ndarray[:, 0]]
+    return faces, [(f, mesh.fccls[f, 0], mesh.fccls[f, 1]) for f in faces]
+
+
+@pytest.mark.parametrize("name", ["tri3", "quad1", "mixed", "tet1", "hex1",
+                                  "prism1", "pyr1"])
+def test_boundary_conditions(name):
+    mesh = fixture_mesh(name)
+    nd, neq = mesh.ndim, mesh.ndim + 2
+    faces, bnd = _bnd(mesh)
+    eye = np.eye(nd)
+    # normal matrix: orthonormal, first row the outward normal.
+    ec = _core(mesh)
+    for f in faces:
+        mat = np.array(ec.get_normal_matrix(f))
+        np.testing.assert_allclose(mat @ mat.T, eye, atol=1e-12)
+        np.testing.assert_allclose(mat[0], [mesh.fcnml[f, d]
+                                            for d in range(nd)], atol=1e-12)
+        np.testing.assert_allclose(np.linalg.det(mat), 1.0, atol=1e-12)
+    with pytest.raises(IndexError):
+        ec.get_normal_matrix(10 ** 7)
+    # non-reflective
+    ec = _core(mesh)
+    body = np.array(ec.so0n.ndarray)
+    for icl in range(ec.ncell):
+        body[icl + ec.ngstcell] = [1.0 + 0.1 * icl + 0.37 * k
+                                   for k in range(neq)]
+    ec.so0n.ndarray[...] = body
+    g1 = np.array(ec.so1c.ndarray)
+    for icl in range(ec.ncell):
+        for k in range(neq):
+            for d in range(nd):
+                g1[icl + ec.ngstcell, k, d] = 0.2 + 0.1 * k - 0.05 * d + \
+                    0.03 * icl
+    ec.so1c.ndarray[...] = g1
+    ec.add_nonrefl(faces)
+    ec.bc_soln()
+    ec.bc_dsoln()
+    for f, icl, jcl in bnd:
+        n = np.array([mesh.fcnml[f, d] for d in range(nd)])
+        np.testing.assert_allclose(ec.so0n[jcl], ec.so0n[icl], rtol=1e-15)
+        gi, gg = ec.so1c[icl], ec.so1n[jcl]
+        np.testing.assert_allclose(gg, gi - np.outer(gi @ n, n), atol=1e-12)
+    # slip wall
+    ec.clear_bc()
+    ec.add_slipwall(faces)
+    ec.bc_soln()
+    ec.bc_dsoln()
+    for f, icl, jcl in bnd:
+        n = np.array([mesh.fcnml[f, d] for d in range(nd)])
+        refl = eye - 2.0 * np.outer(n, n)
+        mi, mg = ec.so0n[icl][1:1 + nd], ec.so0n[jcl][1:1 + nd]
+        np.testing.assert_allclose(mg, refl @ mi, atol=1e-12)
+        assert ec.so0n[jcl, 0] == ec.so0n[icl, 0]
+        assert ec.so0n[jcl, neq - 1] == ec.so0n[icl, neq - 1]
+        for k in (0, neq - 1):
+            np.testing.assert_allclose(ec.so1n[jcl][k], refl @ ec.so1c[icl][k],
+                                       atol=1e-12)
+        gmi = ec.so1c[icl][1:1 + nd]
+        np.testing.assert_allclose(ec.so1n[jcl][1:1 + nd], refl @ gmi @ refl,
+                                   atol=1e-12)
+    # inlet
+    ec.clear_bc()
+    val = [1.3] + [2.0, 0.3, -0.1][:nd] + [0.8, GAMMA]
+    ec.add_inlet(faces, value=val)
+    ec.bc_soln()
+    ec.bc_dsoln()
+    en = 0.8 / (GAMMA - 1.0) + 0.5 * 1.3 * sum(c * c for c in val[1:1 + nd])
+    for f, icl, jcl in bnd:
+        np.testing.assert_allclose(
+            ec.so0n[jcl], [1.3] + [1.3 * c for c in val[1:1 + nd]] + [en])
+        assert not np.any(ec.so1n[jcl])
+    # validation
+    with pytest.raises(ValueError):
+        ec.add_inlet(faces, value=[1.0] * (nd + 2))
+    for bad in ([0.0] + [0.0] * nd + [1.0, 1.4],
+                [1.0] + [0.0] * nd + [-1.0, 1.4],
+                [1.0] + [0.0] * nd + [1.0, 1.0]):
+        with pytest.raises(ValueError):
+            ec.add_inlet(faces, value=bad)
+    with pytest.raises(ValueError):
+        ec.add_nonrefl([10 ** 7])
+
+
+def test_channel_march_bounded():
+    lx, ly = 4.0, 2.0
+    mesh = quad_channel(4, 2, lx, ly)
+    left, right, walls = [], [], []
+    for f in mesh.bndfcs.ndarray[:, 0]:
+        f = int(f)
+        cx = mesh.fccnd[f, 0]
+        (left if abs(cx) < 1e-9 else right if abs(cx - lx) < 1e-9
+         else walls).append(f)
+    ec = _core(mesh, dt=0.04)
+    ec.init_solution(gamma=1.4, rho=1.0, v=[2.0, 0.0], p=1.0)
+    ec.add_inlet(left, value=[1.0, 2.0, 0.0, 1.0, 1.4])
+    ec.add_nonrefl(right)
+    ec.add_slipwall(walls)
+    ec.bc_soln()
+    ec.bc_dsoln()
+    ec.march(steps=5)
+    so0n = np.array(ec.so0n.ndarray)
+    assert np.all(np.isfinite(so0n))
+    np.testing.assert_allclose(so0n[ec.ngstcell:, 0], 1.0, atol=1e-6)
+    for f in left:
+        np.testing.assert_allclose(ec.so0n[mesh.fccls[f, 1], 0], 1.0)
+
+
+# -- parity with the oracle ---------------------------------------------------
+
+def _meshes():
+    from solvcon_gb300 import meshgen
+    out = {}
+    for name, (nd, gen, args) in {
+            "tri": (2, meshgen.tri_square, (7, 0.2, 4)),
+            "quad": (2, meshgen.quad_square, (6, 0.15, 5)),
+            "tet": (3, meshgen.tet_cube, (2, 0.15, 6)),
+            "hex": (3, meshgen.hex_cube, (3, 0.1, 7)),
+            "prism": (3, meshgen.prism_slab, (3, 2, 0.1, 8))}.items():
+        x, t, c = gen(*args)
+        out[name] = meshgen.build_mesh(nd, x, t, c)
+    for name in ("mixed", "pyr1", "prism1"):
+        out[name] = fixture_mesh(name)
+    return out
+
+
+_MESHES = None
+
+
+def meshes():
+    global _MESHES
+    if _MESHES is None:
+        _MESHES = _meshes()
+    return _MESHES
+
+
+MESH_NAMES = ["tri", "quad", "tet", "hex", "prism", "mixed", "pyr1", "prism1"]
+
+
+def _random_state(ec, seed):
+    rng = np.random.default_rng(seed)
+    nd, neq = ec.ndim, ec.neq
+    tot = ec.ncell + ec.ngstcell
+    rho = rng.uniform(0.5, 1.5, tot)
+    v = rng.uniform(-0.5, 0.5, (tot, nd))
+    p = rng.uniform(0.5, 1.5, tot)
+    from solvcon_gb300 import meshgen
+    so0 = meshgen.conserved(rho, v, p, GAMMA)
+    so1 = rng.uniform(-0.3, 0.3, (tot, neq, nd))
+    so0t = rng.uniform(-0.3, 0.3, (tot, neq))
+    return so0, so1, so0t
+
+
+def _pair(name, dt=0.01, precision="fp64"):
+    from oracle import oracle as ora
+    mesh = meshes()[name]
+    return mesh, _core(mesh, dt, precision), ora.OracleEuler(mesh, dt)
+
+
+def _load(ec, ref, **arrays):
+    for k, v in arrays.items():
+        getattr(ec, k).ndarray[...] = v
+        getattr(ref, k)[...] = v
+
+
+@pytest.mark.parametrize("name", MESH_NAMES)
+def test_prepare_ce_matches_oracle(name):
+    mesh, ec, ref = _pair(name)
+    for a in ("cevol", "cecnd", "sfcnd", "sfnml"):
+        assert_rel(ec.__getattribute__(a).ndarray, getattr(ref, a), 1e-14, a)
+
+
+@pytest.mark.parametrize("name", MESH_NAMES)
+def test_each_operation_matches_oracle(name):
+    mesh, ec, ref = _pair(name)
+    so0, so1, so0t = _random_state(ec, 11)
+    gamma = np.full(ec.ncell + ec.ngstcell, GAMMA)
+    _load(ec, ref, so0c=so0, so1c=so1, so0t=so0t, gamma=gamma)
+    ec.calc_solt()
+    ref.call("calc_solt")
+    assert_rel(ec.so0t.ndarray, ref.so0t, 1e-12, "calc_solt")
+    _load(ec, ref, so0t=so0t)
+    ec.calc_soln()
+    ref.call("calc_soln")
+    ng = ec.ngstcell
+    assert_rel(np.array(ec.so0n.ndarray)[ng:], ref.so0n[ng:], 1e-12,
+               "calc_soln")
+    _load(ec, ref, so0n=np.array(ref.so0n))
+    ec.calc_cfl()
+    ref.call("calc_cfl")
+    assert_rel(ec.cflo.ndarray, ref.cflo, 1e-13, "cflo")
+    assert_rel(ec.cflc.ndarray, ref.cflc, 1e-13, "cflc")
+    assert_rel(ec.so0n.ndarray, ref.so0n, 1e-13, "cfl energy")
+    _load(ec, ref, so0n=np.array(ref.so0n), cflc=np.array(ref.cflc))
+    ec.calc_dsoln()
+    ref.call("calc_dsoln")
+    assert_rel(np.array(ec.so1n.ndarray)[ng:], ref.so1n[ng:], 1e-11,
+               "calc_dsoln")
+    mask = ec.limiter_mask()
+    assert np.array_equal(mask, ref.limiter[:ec.ncell])
+    faces = [int(f) for f in mesh.bndfcs.ndarray[:, 0]]
+    for kind in (0, 1, 2):
+        _load(ec, ref, so1c=so1)
+        ec.clear_bc()
+        ref._bcs = []
+        val = [1.3] + [0.4, -0.2, 0.1][:ec.ndim] + [0.8, GAMMA]
+        half = faces[: max(1, len(faces) // 2)]
+        ec._add_bc(kind, half, val if kind == 2 else ())
+        ref.add_bc(kind, half, val if kind == 2 else ())
+        ec.bc_soln()
+        ec.bc_dsoln()
+        ref.call("bc_soln")
+        ref.call("bc_dsoln")
+        assert_rel(ec.so0n.ndarray, ref.so0n, 1e-14, "bc_soln %d" % kind)
+        assert_rel(ec.so1n.ndarray, ref.so1n, 1e-14, "bc_dsoln %d" % kind)
+
+
+@pytest.mark.parametrize("name", MESH_NAMES)
+def test_march_matches_oracle(name):
+    from solvcon_gb300 import meshgen
+    mesh, ec, ref = _pair(name, dt=2e-3)
+    ng = ec.ngstcell
+    clcnd = np.array(mesh.clcnd.ndarray)[ng:]
+    if mesh.ndim == 2:
+        state = meshgen.quadrant_state(clcnd[:, :2], seed=9)
+    else:
+        state = meshgen.blast_state(clcnd, radius=0.4)
+    faces = [int(f) for f in mesh.bndfcs.ndarray[:, 0]]
+    for core in (ec, ref):
+        core.init_solution(GAMMA, 1.0, [0.0] * mesh.ndim, 1.0)
+        core.add_slipwall(faces)
+    ec.so0n.ndarray[ng:] = state
+    ref.so0n[ng:] = state
+    ec.bc_soln()
+    ec.bc_dsoln()
+    ref.call("bc_soln")
+    ref.call("bc_dsoln")
+    ec.march(4)
+    ref.march(4)
+    for a in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo", "cflc"):
+        assert_rel(getattr(ec, a).ndarray, getattr(ref, a), 1e-10, a)
+    ec.march_substep()
+    ref.call("march_substep")
+    for a in ("so0n", "so1n", "so0t"):
+        assert_rel(getattr(ec, a).ndarray, getattr(ref, a), 1e-10, a)
+    tot = ec.totals()
+    vol = np.array(mesh.clvol.ndarray)[ng:]
+    want = (np.array(ref.so0n)[ng:] * vol[:, None]).sum(axis=0)
+    np.testing.assert_allclose(tot, want, rtol=1e-12)
+    lo, hi = ec.cfl_range()
+    np.testing.assert_allclose([lo, hi], [ref.cflo[ng:].min(),
+                                          ref.cflo[ng:].max()], rtol=1e-12)
+
+
+def test_march_matches_reference_golden():
+    """The march of the golden fixtures generated from the reference."""
+    from _util import golden
+    from test_mesh import _build
+    for case in ("tri12", "quad8", "tet3"):
+        gm = golden("mesh_" + case)
+        g = golden("march_" + case)
+        mesh = _build(gm)
+        ec = _core(mesh, dt=float(g["dt"]))
+        ec.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+        ec.so0n.ndarray[ec.ngstcell:] = g["state0"]
+        ec._add_bc(int(g["bc_kind"]), g["faces"])
+        ec.bc_soln()
+        ec.bc_dsoln()
+        ec.march(int(g["steps"]))
+        for a in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo", "cflc"):
+            assert_rel(getattr(ec, a).ndarray, g[a], 1e-10, case + " " + a)

@@ -1,0 +1,125 @@
+"""Pin the CPU oracle before trusting it.
+
+The oracle (oracle/cese_oracle.c) restates the reference march; here it is
+checked against the golden vectors produced by the reference itself
+(tests/golden/, made by tests/golden/make_golden.py), against the reference
+library directly where it is built on this host (oracle/_ref), and against
+the known-answer properties the reference's own tests assert.
+"""
+
+import numpy as np
+import pytest
+
+from _util import golden
+from test_mesh import _build
+
+
+def _oracle_from_golden(case):
+    from oracle import oracle as ora
+    gm = golden("mesh_" + case)
+    g = golden("march_" + case)
+    mesh = _build(gm)
+    o = ora.OracleEuler(mesh, float(g["dt"]))
+    o.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+    o.so0n[o.ngstcell:] = g["state0"]
+    o.add_bc(int(g["bc_kind"]), g["faces"])
+    o.call("bc_soln")
+    o.call("bc_dsoln")
+    return mesh, o, g
+
+
+@pytest.mark.parametrize("case", ["tri12", "quad8", "tet3"])
+def test_oracle_reproduces_reference_march(case):
+    mesh, o, g = _oracle_from_golden(case)
+    for a in ("cevol", "cecnd"):
+        np.testing.assert_array_equal(getattr(o, a), g[a])
+    o.march(int(g["steps"]))
+    for a in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo", "cflc"):
+        np.testing.assert_allclose(getattr(o, a), g[a], rtol=0, atol=1e-13,
+                                   err_msg=a)
+
+
+def test_oracle_reproduces_reference_sod():
+    from oracle import oracle as ora
+    g = golden("e1d_sod")
+    n = g["coord"].size
+    o = ora.OracleEuler1D(n, float(g["dt"]))
+    o.coord[:] = g["coord"]
+    o.so0[:] = g["so0_in"]
+    o.gamma[:] = 1.4
+    o.setup_march()
+    o.march_alpha(2, int(g["steps"]))
+    for a in ("so0", "so1", "cfl"):
+        np.testing.assert_allclose(getattr(o, a), g[a], rtol=0, atol=1e-14)
+
+
+def test_oracle_free_stream_and_linear_field():
+    """Known answers of the reference tests (tests/test_multidim.py:657-708):
+    a uniform state is preserved exactly; a linear field's gradient is
+    recovered exactly."""
+    from oracle import oracle as ora
+    from solvcon_gb300 import meshgen
+    x, t, c = meshgen.tri_square(6, 0.2, 2)
+    mesh = meshgen.build_mesh(2, x, t, c)
+    o = ora.OracleEuler(mesh, 0.01)
+    row = np.array([1.2, 0.36, -0.18, 0.9 / 0.4 + 0.5 * 1.2 * 0.1125])
+    o.gamma[:] = 1.4
+    o.so0c[:] = row
+    o.so1c[:] = 0.0
+    o.call("calc_solt")
+    o.call("calc_soln")
+    np.testing.assert_allclose(o.so0n[o.ngstcell:], np.broadcast_to(
+        row, (o.ncell, 4)), rtol=1e-12)
+    g = np.array([[0.1 * (i + 1) + 0.01 * (d + 1) for d in range(2)]
+                  for i in range(4)])
+    ng = o.ngstcell
+    pts = np.array(o.cecnd[:, :2])
+    pts[:ng] = np.array(mesh.clcnd.ndarray)[:ng]
+    vals = 0.5 + pts @ g.T
+    o.so0c[:] = vals
+    o.so0n[:] = vals
+    o.so0t[:] = 0.0
+    o.so1c[:] = g[None]
+    o.cflc[:] = 0.5
+    o.call("calc_dsoln")
+    np.testing.assert_allclose(o.so1n[ng:], np.broadcast_to(g, (o.ncell, 4, 2)),
+                               rtol=1e-9)
+
+
+def test_oracle_against_reference_library():
+    from oracle import oracle as ora
+    from oracle import refbind as rb
+    if not rb.available():
+        pytest.skip("reference library not built on this host")
+    from solvcon_gb300 import meshgen
+    for nd, (x, t, c) in ((2, meshgen.quad_square(7, 0.2, 3)),
+                          (3, meshgen.hex_cube(2, 0.1, 3)),
+                          (3, meshgen.prism_slab(3, 2, 0.1, 3))):
+        mesh = meshgen.build_mesh(nd, x, t, c)
+        r = rb.RefMesh(nd, x, t, c)
+        ref = rb.RefEuler(r, 3e-3)
+        o = ora.OracleEuler(mesh, 3e-3)
+        ng = o.ngstcell
+        clcnd = np.array(mesh.clcnd.ndarray)[ng:]
+        st = meshgen.quadrant_state(clcnd[:, :2], 4) if nd == 2 else \
+            meshgen.blast_state(clcnd, radius=0.4)
+        st = st if nd == 2 else st
+        for core in (o, ref):
+            core.init_solution(1.4, 1.0, [0.0] * nd, 1.0)
+        so = ref.get("so0n")
+        so[ng:] = st
+        ref.set("so0n", so)
+        o.so0n[ng:] = st
+        faces = np.array(mesh.bndfcs.ndarray[:, 0])
+        ref.add_bc(0, faces[::2])
+        o.add_bc(0, faces[::2])
+        ref.add_bc(1, faces[1::2])
+        o.add_bc(1, faces[1::2])
+        ref.call("bc_soln")
+        ref.call("bc_dsoln")
+        o.call("bc_soln")
+        o.call("bc_dsoln")
+        ref.march(3)
+        o.march(3)
+        for a in ("so0n", "so1n", "so0t", "cflc"):
+            np.testing.assert_array_equal(getattr(o, a), ref.get(a), a)
