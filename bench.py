@@ -1,0 +1,451 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU CESE march: cell-steps/s on the 2D plain-FP64 workload.
+
+Workload (default, ``--workload tri2d``): the unit square cut into
+1000 x 1000 quads, each split on the same diagonal into 2 triangles
+(2,000,000 cells), interior nodes jittered by U(-0.2h, 0.2h) from a seed;
+four-quadrant Riemann state (rho, p in [0.1, 1.5], |u|, |v| <= 0.8) from a
+seed; gamma 1.4; slip walls on every boundary face; dt set for CFL 0.8 from a
+probe calc_cfl; plain FP64.  One bench "step" is one full march step (two
+CESE substeps) of the whole mesh.  The state (about 1.3 GB with geometry) is
+far larger than the 129 MB L2, so no flush is needed between steps.
+
+Printed (one JSON line on rank 0): ``value`` = cell-steps/s with the state
+resident in HBM; ``e2e`` = the same metric through the C ABI with the state in
+pinned host memory copied in and out every step; ``roofline`` of the fused
+substep kernel (HBM bytes are the algorithmic bytes of one cell-substep); the
+FP64-pipe roofline beside it; ``cpu_baseline`` = the CPU oracle on a bounded
+sample; clocks sampled during the timed region.
+
+``--impl reference`` times the reference algorithm on the host CPU instead
+(the C oracle, a restatement of the reference march: the reference itself
+cannot be built on the GPU host, which has no copy of its sources).
+Under torchrun with N > 1 every rank marches its own mesh (replicas: a single
+mesh is not decomposed), times are maxed over ranks and the value is the sum.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic HBM bytes of one cell-substep of the fused march: compulsory
+# reads of the neighbour-summed state, the cell's geometry and ids, and writes
+# of so0n, so1n, cflo, cflc (FP64, 2D triangles: 520 B; 3D tetrahedra:
+# 1,100 B; FP32 state with FP64 geometry: 412 B / 928 B).
+ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
+             ("tri2d", "fp32"): 412, ("tet3d", "fp64"): 1100,
+             ("tet3d", "fp32-geom64"): 928, ("tet3d", "fp32"): 928}
+
+# DRAM bytes (read + write) and FP64 flops (DFMA counted as 2) of the fused
+# substep kernel per cell-substep, from one ncu capture each
+# (profiles/fused_substep_tri2d_fp64.md); absent until captured.
+NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 611.3}
+NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1446.8}
+
+WORKLOADS = {
+    "tri2d": dict(ndim=2, nside=1000, jitter=0.2, cfl=0.8, seed=2026),
+    "tet3d": dict(ndim=3, nside=160, jitter=0.15, cfl=0.7, seed=2026),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" +
+                 self.QUERY, "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name, nside=None, seed_offset=0):
+    from solvcon_gb300 import meshgen
+    w = dict(WORKLOADS[name])
+    if nside:
+        w["nside"] = nside
+    if w["ndim"] == 2:
+        x, t, c = meshgen.tri_square(w["nside"], w["jitter"],
+                                     w["seed"] + seed_offset)
+    else:
+        x, t, c = meshgen.tet_cube(w["nside"], w["jitter"],
+                                   w["seed"] + seed_offset)
+    mesh = meshgen.build_mesh(w["ndim"], x, t, c)
+    clcnd = np.asarray(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    if w["ndim"] == 2:
+        state = meshgen.quadrant_state(clcnd, seed=w["seed"] + seed_offset)
+    else:
+        state = meshgen.blast_state(clcnd)
+    faces = np.asarray(mesh.bndfcs.ndarray[:, 0]).copy()
+    return w, mesh, state, faces
+
+
+def dt_for_cfl(mesh, state, faces, cfl, precision="fp64"):
+    """dt giving max(cflo) = cfl for the initial state (cflo is linear in
+    dt): a probe core with dt = 1 runs calc_cfl."""
+    import solvcon_gb300 as sg
+    probe = sg.EulerCore(mesh, 1.0, precision=precision)
+    probe.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+    probe.so0n.ndarray[probe.ngstcell:] = state
+    probe.calc_cfl()
+    cmax = probe.cfl_range()[1]
+    del probe
+    return cfl / cmax
+
+
+def setup_core(mesh, state, faces, dt, precision):
+    import solvcon_gb300 as sg
+    core = sg.EulerCore(mesh, dt, precision=precision)
+    core.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+    core.add_slipwall(faces)
+    core.so0n[0:] = state
+    core.bc_soln()
+    core.bc_dsoln()
+    core.release_views()
+    core.sync()
+    return core
+
+
+def time_resident(core, steps):
+    """K march steps on the core's stream, CUDA events on that stream."""
+    from solvcon_gb300._lib import check, launch_count, lib
+    stream = ctypes.c_void_p()
+    check(lib.scg_euler_stream(core.handle, ctypes.byref(stream)))
+    e0, e1 = ctypes.c_void_p(), ctypes.c_void_p()
+    check(lib.scg_event_create(ctypes.byref(e0)))
+    check(lib.scg_event_create(ctypes.byref(e1)))
+    check(lib.scg_euler_profile(core.handle, 1))
+    core.sync()
+    n0 = launch_count()
+    check(lib.scg_event_record(e0, stream))
+    core.march_async(steps)
+    check(lib.scg_event_record(e1, stream))
+    ms = ctypes.c_double()
+    check(lib.scg_event_elapsed(e0, e1, ctypes.byref(ms)))
+    launches = launch_count() - n0
+    kms = ctypes.c_double()
+    kn = ctypes.c_int64()
+    check(lib.scg_euler_profile_stats(core.handle, ctypes.byref(kms),
+                                      ctypes.byref(kn)))
+    check(lib.scg_euler_profile(core.handle, 0))
+    check(lib.scg_event_destroy(e0))
+    check(lib.scg_event_destroy(e1))
+    return ms.value, launches, kms.value, kn.value
+
+
+def time_e2e(core, steps):
+    """K steps through the C ABI with host state: per step the state (so0n,
+    so1n) is copied from pinned host memory, one march step runs, and the new
+    state is read back into the same pinned buffers.  Wall time around the
+    whole loop."""
+    from solvcon_gb300._lib import check, lib
+    ids = {"so0n": 5, "so1n": 8}
+    bufs = {}
+    for name in ("so0n", "so1n"):
+        arr = np.array(getattr(core, name)[...])
+        p = ctypes.c_void_p()
+        check(lib.scg_host_alloc(arr.nbytes, ctypes.byref(p)))
+        view = np.ctypeslib.as_array((ctypes.c_double * arr.size)
+                                     .from_address(p.value)).reshape(arr.shape)
+        view[...] = arr
+        bufs[name] = (p, view)
+    h2d = bufs["so0n"][1].nbytes + bufs["so1n"][1].nbytes
+    d2h = h2d
+    h = core.handle
+    core.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for name in ("so0n", "so1n"):
+            p, view = bufs[name]
+            check(lib.scg_euler_set(h, ids[name], p, view.size))
+        check(lib.scg_euler_march(h, 1))
+        for name in ("so0n", "so1n"):
+            p, view = bufs[name]
+            check(lib.scg_euler_get(h, ids[name], p, view.size))
+    t1 = time.perf_counter()
+    for p, _ in bufs.values():
+        check(lib.scg_host_free(p))
+    return (t1 - t0) * 1e3, h2d, d2h
+
+
+def cpu_baseline(workload, nside, steps):
+    """The CPU oracle (restatement of the reference march) on a bounded
+    sample: the same generator at a smaller resolution, one core."""
+    from oracle import oracle as ora
+    w, mesh, state, faces = make_workload(workload, nside=nside)
+    dt = 1e-4
+    o = ora.OracleEuler(mesh, dt)
+    o.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+    o.so0n[o.ngstcell:] = state
+    o.add_slipwall(faces)
+    o.call("bc_soln")
+    o.call("bc_dsoln")
+    t0 = time.perf_counter()
+    o.march(steps)
+    t1 = time.perf_counter()
+    return mesh.ncell * steps / (t1 - t0), mesh.ncell, t1 - t0
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def reduce_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    nside = args.cpu_nside or (300 if w["ndim"] == 2 else 20)
+    from oracle import oracle as ora
+    ww, mesh, state, faces = make_workload(args.workload, nside=nside)
+    o = ora.OracleEuler(mesh, 1e-4)
+    o.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
+    o.so0n[o.ngstcell:] = state
+    o.add_slipwall(faces)
+    o.call("bc_soln")
+    o.call("bc_dsoln")
+    o.march(args.warmup)
+    t0 = time.perf_counter()
+    o.march(args.steps)
+    t1 = time.perf_counter()
+    value = mesh.ncell * args.steps / (t1 - t0)
+    sample = ("%d-cell sample of the %s workload (same generator, nside=%d), "
+              "%d march steps, 1 thread (the reference march is serial)"
+              % (mesh.ncell, args.workload, nside, args.steps))
+    line = {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
+        "impl": "reference", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": (t1 - t0) * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "%s (%s)" % (args.workload, _desc(w)),
+                   "sample_cells": mesh.ncell, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": 1,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cell-steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _desc(w):
+    if w["ndim"] == 2:
+        return ("2D Euler, unit square %dx%d quads x 2 triangles = %d cells, "
+                "jitter %.2fh, four-quadrant Riemann state, slip walls, "
+                "CFL %.1f" % (w["nside"], w["nside"], 2 * w["nside"] ** 2,
+                              w["jitter"], w["cfl"]))
+    return ("3D Euler, unit cube %d^3 hexes x 6 tetrahedra = %d cells, jitter "
+            "%.2fh, spherical blast, slip walls, CFL %.1f" %
+            (w["nside"], 6 * w["nside"] ** 3, w["jitter"], w["cfl"]))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tri2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default=None,
+                    choices=["fp64", "fp32", "fp32-geom64"])
+    ap.add_argument("--nside", type=int, default=None)
+    ap.add_argument("--cpu-nside", type=int, default=None)
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        return
+    precision = args.precision or ("fp64" if args.workload == "tri2d"
+                                   else "fp32")
+
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    import solvcon_gb300  # noqa: F401  (fails loudly without libscg.so)
+    from solvcon_gb300._lib import check, lib
+
+    t_setup = time.perf_counter()
+    w, mesh, state, faces = make_workload(args.workload, args.nside,
+                                          seed_offset=rank)
+    dt = dt_for_cfl(mesh, state, faces, w["cfl"], precision)
+    core = setup_core(mesh, state, faces, dt, precision)
+    t_setup = time.perf_counter() - t_setup
+    ncell = core.ncell
+
+    core.march(args.warmup)
+    fp64_peak = ctypes.c_double()
+    check(lib.scg_fma_peak(0, 4000, ctypes.byref(fp64_peak)))
+    barrier(dist)
+    with ClockSampler(local) as clocks:
+        ms, launches, kms, kn = time_resident(core, args.steps)
+    barrier(dist)
+    ms_max = reduce_max(dist, ms)
+    value = world * ncell * args.steps / (ms_max * 1e-3)
+
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
+    e2e_ms, h2d, d2h = time_e2e(core, e2e_steps)
+    e2e_ms = reduce_max(dist, e2e_ms)
+    e2e_value = world * ncell * e2e_steps / (e2e_ms * 1e-3)
+    finite = bool(np.all(np.isfinite(np.array(core.so0n.ndarray))))
+    lo, hi = core.cfl_range()
+
+    hbm_peak, peak_kind = peaks()
+    per_launch_ms = kms / max(kn, 1)
+    key = (args.workload, precision)
+    alg = ALG_BYTES[key] * ncell
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    traffic = NCU_TRAFFIC_PER_CELL.get(key)
+    dp_flops = NCU_DP_FLOPS_PER_CELL.get(key)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+        "unit": "GB/s", "frac": achieved / hbm_peak,
+        "traffic": traffic * ncell if traffic else None,
+        "kernel": "k_fused (one CESE substep)",
+        "alg_bytes_per_cell_substep": ALG_BYTES[key],
+        "launch_ms": per_launch_ms, "launches_timed": kn,
+        "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+        if peak_kind == "measured" else "fallback 6.8 TB/s",
+        "fp64": {"peak_tflops": fp64_peak.value,
+                 "peak_source": "measured live (scg_fma_peak FP64 FMA chain)",
+                 "flops_per_cell_substep": dp_flops,
+                 "achieved_tflops": (dp_flops * ncell /
+                                     (per_launch_ms * 1e-3) / 1e12
+                                     if dp_flops else None),
+                 "frac": (dp_flops * ncell / (per_launch_ms * 1e-3) / 1e12 /
+                          fp64_peak.value if dp_flops else None)},
+    }
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nside = args.cpu_nside or (300 if w["ndim"] == 2 else 20)
+        rate, ncpu, secs = cpu_baseline(args.workload, nside, args.cpu_steps)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": 1,
+               "kind": "port",
+               "sample": "%d-cell sample (same generator, nside=%d), %d march "
+                         "steps, %.1f s, 1 thread" % (ncpu, nside,
+                                                      args.cpu_steps, secs)}
+
+    line = {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == "fp64" else "f32",
+        "data": "synthetic",
+        "config": {"workload": "%s (%s)" % (args.workload, _desc(w)),
+                   "cells": ncell, "precision": precision, "dt": dt,
+                   "l2": "state larger than L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "setup_s": t_setup},
+        "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "cell-steps/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+        "gpu_launches": launches, "clocks": clocks.summary(),
+        "check": {"finite": finite, "cflo_range": [lo, hi]},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -186,6 +186,31 @@ int scg_euler_cfl_range(scg_euler * core, double * out);
 /* Device memory held by the core, in bytes. */
 int scg_euler_device_bytes(const scg_euler * core, int64_t * out);
 
+/* The core's CUDA stream (cudaStream_t) for stream-ordered event timing. */
+int scg_euler_stream(const scg_euler * core, void ** out);
+/* Per-launch CUDA-event timing of the fused march kernel: enable (resets the
+ * record) or disable; stats return the summed duration and launch count. */
+int scg_euler_profile(scg_euler * core, int on);
+int scg_euler_profile_stats(scg_euler * core, double * ms_total, int64_t * launches);
+
+/* ------------------------------------------------------------------------
+ * Timing and host-memory helpers (no reference counterpart: measurement
+ * plumbing of this library).
+ * ---------------------------------------------------------------------- */
+
+/* Device FMA throughput in TFLOP/s for SCG_FP64 or SCG_FP32 (a register-only
+ * FMA chain over all SMs, iters FMAs-per-accumulator). */
+int scg_fma_peak(int precision, int iters, double * tflops);
+/* Page-locked host buffers for end-to-end host<->device copies. */
+int scg_host_alloc(int64_t nbytes, void ** out);
+int scg_host_free(void * ptr);
+/* CUDA events (cudaEvent_t) recorded on a stream, and their elapsed time. */
+int scg_event_create(void ** out);
+int scg_event_destroy(void * ev);
+int scg_event_record(void * ev, void * stream);
+int scg_event_elapsed(void * ev0, void * ev1, double * ms);
+int scg_device_sync(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,17 @@ _SIGS = {
     "scg_euler_totals": ([_vp, _vp], ctypes.c_int),
     "scg_euler_cfl_range": ([_vp, _vp], ctypes.c_int),
     "scg_euler_device_bytes": ([_vp, _vp], ctypes.c_int),
+    "scg_euler_stream": ([_vp, _vp], ctypes.c_int),
+    "scg_euler_profile": ([_vp, ctypes.c_int], ctypes.c_int),
+    "scg_euler_profile_stats": ([_vp, _vp, _vp], ctypes.c_int),
+    "scg_fma_peak": ([ctypes.c_int, ctypes.c_int, _vp], ctypes.c_int),
+    "scg_host_alloc": ([ctypes.c_int64, _vp], ctypes.c_int),
+    "scg_host_free": ([_vp], ctypes.c_int),
+    "scg_event_create": ([_vp], ctypes.c_int),
+    "scg_event_destroy": ([_vp], ctypes.c_int),
+    "scg_event_record": ([_vp, _vp], ctypes.c_int),
+    "scg_event_elapsed": ([_vp, _vp, _vp], ctypes.c_int),
+    "scg_device_sync": ([], ctypes.c_int),
 }
 
 EXPORTED = tuple(_SIGS)

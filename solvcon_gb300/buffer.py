@@ -21,15 +21,17 @@ class SimpleArray:
     :param fetch: callable returning the whole numpy buffer (ghost rows
         first); it is called on every access so the owner can refresh it.
     :param nghost: ghost rows on the first axis.
-    :param on_write: called after every write made through this view and
-        whenever :attr:`ndarray` hands the buffer out (the caller may write
-        through it).
+    :param on_write: called after every write made through this view.
+    :param on_expose: called whenever :attr:`ndarray` hands the buffer out
+        (the caller may keep it and write through it at any time); defaults
+        to ``on_write``.
     """
 
-    def __init__(self, fetch, nghost=0, on_write=None):
+    def __init__(self, fetch, nghost=0, on_write=None, on_expose=None):
         self._fetch = fetch
         self._nghost = int(nghost)
         self._on_write = on_write
+        self._on_expose = on_expose if on_expose is not None else on_write
 
     # -- buffer -------------------------------------------------------------
 
@@ -40,8 +42,8 @@ class SimpleArray:
     def ndarray(self):
         """The whole buffer, ghost rows first (writes go to the table)."""
         buf = self._buf()
-        if self._on_write is not None:
-            self._on_write()
+        if self._on_expose is not None:
+            self._on_expose()
         return buf
 
     def __array__(self, dtype=None, copy=None):

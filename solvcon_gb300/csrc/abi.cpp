@@ -362,4 +362,19 @@ int scg_euler_device_bytes(const scg_euler * core, int64_t * out)
     return guarded([&] { *out = static_cast<int64_t>(need(core, "scg_euler_device_bytes")->c->device_bytes()); });
 }
 
+int scg_euler_stream(const scg_euler * core, void ** out)
+{
+    return guarded([&] { *out = need(core, "scg_euler_stream")->c->get_stream(); });
+}
+
+int scg_euler_profile(scg_euler * core, int on)
+{
+    return guarded([&] { need(core, "scg_euler_profile")->c->profile(on != 0); });
+}
+
+int scg_euler_profile_stats(scg_euler * core, double * ms_total, int64_t * launches)
+{
+    return guarded([&] { need(core, "scg_euler_profile_stats")->c->profile_stats(ms_total, launches); });
+}
+
 } // extern "C"

@@ -18,6 +18,8 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace scg
 {
@@ -587,6 +589,11 @@ public:
 
     ~EulerCoreImpl() override
     {
+        for (auto & pr : prof_events)
+        {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
         if (own_stream)
         {
             cudaStreamSynchronize(own_stream);
@@ -615,6 +622,34 @@ public:
     }
 
     void sync() override { cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+
+    cudaStream_t get_stream() const override { return stream; }
+
+    void profile(bool on) override
+    {
+        sync();
+        for (auto & pr : prof_events)
+        {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+        prof_events.clear();
+        profiling = on;
+    }
+
+    void profile_stats(double * ms_total, int64_t * launches) override
+    {
+        sync();
+        double tot = 0.0;
+        for (auto & pr : prof_events)
+        {
+            float f = 0.f;
+            cuda_check(cudaEventElapsedTime(&f, pr.first, pr.second), "elapsed");
+            tot += f;
+        }
+        *ms_total = tot;
+        *launches = static_cast<int64_t>(prof_events.size());
+    }
 
     // ---- geometry -------------------------------------------------------
 
@@ -811,16 +846,17 @@ public:
         {
             return;
         }
-        DevBuf<double> tmp(static_cast<size_t>(n));
+        double * const tmp = staging(n);
+        size_t const nb = static_cast<size_t>(n) * sizeof(double);
         if (which >= EA_CEVOL && which <= EA_SFNML)
         {
             ensure_ce();
-            cuda_check(cudaMemcpyAsync(tmp.ptr, ce[which].ptr, tmp.bytes(), cudaMemcpyDeviceToDevice, stream), "copy");
+            cuda_check(cudaMemcpyAsync(tmp, ce[which].ptr, nb, cudaMemcpyDeviceToDevice, stream), "copy");
         }
         else if (which == EA_CFLO || which == EA_CFLC || which == EA_GAMMA)
         {
             R const * src = which == EA_CFLO ? d_cflo.ptr : which == EA_CFLC ? d_cflc.ptr : d_gamma.ptr;
-            k_to_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(src, tmp.ptr, n);
+            k_to_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(src, tmp, n);
             launched(stream, "to_f64");
         }
         else
@@ -828,10 +864,10 @@ public:
             R * base;
             int off, width;
             field_of(which, base, off, width);
-            k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp.ptr, nrow, off, width);
+            k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width);
             launched(stream, "get_field");
         }
-        cuda_check(cudaMemcpyAsync(out, tmp.ptr, tmp.bytes(), cudaMemcpyDeviceToHost, stream), "D2H");
+        cuda_check(cudaMemcpyAsync(out, tmp, nb, cudaMemcpyDeviceToHost, stream), "D2H");
         sync();
     }
 
@@ -848,18 +884,19 @@ public:
         {
             return;
         }
-        DevBuf<double> tmp(static_cast<size_t>(n));
-        cuda_check(cudaMemcpyAsync(tmp.ptr, in, tmp.bytes(), cudaMemcpyHostToDevice, stream), "H2D");
+        double * const tmp = staging(n);
+        size_t const nb = static_cast<size_t>(n) * sizeof(double);
+        cuda_check(cudaMemcpyAsync(tmp, in, nb, cudaMemcpyHostToDevice, stream), "H2D");
         if (which >= EA_CEVOL && which <= EA_SFNML)
         {
             ensure_ce();
-            cuda_check(cudaMemcpyAsync(ce[which].ptr, tmp.ptr, tmp.bytes(), cudaMemcpyDeviceToDevice, stream), "copy");
+            cuda_check(cudaMemcpyAsync(ce[which].ptr, tmp, nb, cudaMemcpyDeviceToDevice, stream), "copy");
             compact();
         }
         else if (which == EA_CFLO || which == EA_CFLC || which == EA_GAMMA)
         {
             R * dst = which == EA_CFLO ? d_cflo.ptr : which == EA_CFLC ? d_cflc.ptr : d_gamma.ptr;
-            k_from_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(tmp.ptr, dst, n);
+            k_from_f64<R><<<grid_for(n), BLOCK, 0, stream>>>(tmp, dst, n);
             launched(stream, "from_f64");
         }
         else
@@ -867,7 +904,7 @@ public:
             R * base;
             int off, width;
             field_of(which, base, off, width);
-            k_set_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp.ptr, nrow, off, width);
+            k_set_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width);
             launched(stream, "set_field");
         }
         next_valid = false;
@@ -1011,8 +1048,20 @@ public:
         }
         if (nrow > 0)
         {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (profiling)
+            {
+                cuda_check(cudaEventCreate(&e0), "event");
+                cuda_check(cudaEventCreate(&e1), "event");
+                cuda_check(cudaEventRecord(e0, stream), "record");
+            }
             k_fused<ND, R, G><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
             launched(stream, "fused_substep");
+            if (profiling)
+            {
+                cuda_check(cudaEventRecord(e1, stream), "record");
+                prof_events.emplace_back(e0, e1);
+            }
             next_valid = true;
             next_buf = cur ^ 1;
         }
@@ -1090,6 +1139,17 @@ public:
     }
 
 private:
+    // Grow-only device staging table for get_array/set_array.
+    double * staging(int64_t n)
+    {
+        if (m_staging.n < static_cast<size_t>(n))
+        {
+            sync();
+            m_staging.alloc(static_cast<size_t>(n));
+        }
+        return m_staging.ptr;
+    }
+
     template <typename T>
     void up(DevBuf<T> & d, std::vector<T> const & h)
     {
@@ -1125,6 +1185,10 @@ private:
     DevBuf<int8_t> d_gkind;
     DevBuf<double> d_gnml, d_gval;
     DevBuf<int32_t> d_gint;
+    DevBuf<double> m_staging;
+
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
 
     int cur = 0;           // index of the current (so0c/so1c) record buffer
     int tbuf = 0;          // buffer holding the logical so0t

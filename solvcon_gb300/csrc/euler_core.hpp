@@ -101,6 +101,10 @@ public:
     // min and max of cflo over body cells.
     virtual void cfl_range(double * out) = 0;
     virtual size_t device_bytes() const = 0;
+    virtual cudaStream_t get_stream() const = 0;
+    // Per-launch CUDA-event timing of the fused substep kernel.
+    virtual void profile(bool on) = 0;
+    virtual void profile_stats(double * ms_total, int64_t * launches) = 0;
 
     void add_bc(int kind, std::vector<int32_t> const & faces, std::vector<double> const & value);
     void clear_bc();

@@ -129,7 +129,12 @@ class EulerCore:
             self._valid.add(name)
         return self._cache[name]
 
-    def _touched(self, name):
+    def _written(self, name):
+        self._dirty.add(name)
+
+    def _exposed_view(self, name):
+        # A caller holding the raw buffer may write through it at any time:
+        # push it before, and refresh it after, every device operation.
         self._dirty.add(name)
         self._exposed.add(name)
 
@@ -164,7 +169,14 @@ class EulerCore:
     def _array(self, name):
         _, ngh = self._shape(_ID[name])
         return SimpleArray(lambda: self._host(name), nghost=ngh,
-                           on_write=lambda: self._touched(name))
+                           on_write=lambda: self._written(name),
+                           on_expose=lambda: self._exposed_view(name))
+
+    def release_views(self):
+        """Stop mirroring the raw buffers handed out by ``arr.ndarray``
+        (writes through them are no longer pushed to the device)."""
+        self._flush()
+        self._exposed.clear()
 
     # -- operations ---------------------------------------------------------
 
