@@ -181,6 +181,18 @@ int scg_euler_limiter_mask(scg_euler * core, uint8_t * out);
  * mass/momentum/energy integrals of solvcon's EulerField
  * (solvcon/multidim/euler/_field.py:16-148). */
 int scg_euler_totals(scg_euler * core, double * out);
+/* The same totals without allocating any memory.  No counterpart in the
+ * reference: it exists for callers that reserved their device memory up front
+ * and must not allocate afterwards (a serving loop polling the totals of every
+ * resident solve under a fixed HBM budget), because scg_euler_totals
+ * allocates a per-call buffer with cudaMalloc and frees it with cudaFree, and
+ * cudaFree synchronises the whole device.  Its partial sums live in a fixed
+ * 131,136-byte device array (held by every GPU that loads the library until
+ * exit) shared by all calls: at most 67,108,864 body cells (larger meshes
+ * are rejected with SCG_EINVAL), the first call on a device looks up the
+ * array's address (make it before any stream capture), and calls that
+ * overlap on the GPU race -- issue them one after the other. */
+int scg_euler_totals_noalloc(scg_euler * core, double * out);
 /* min and max of cflo over body cells (EulerField.calc_cfl_range). */
 int scg_euler_cfl_range(scg_euler * core, double * out);
 /* Device memory held by the core, in bytes. */

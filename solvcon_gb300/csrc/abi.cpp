@@ -33,11 +33,6 @@ struct scg_mesh
     scg::HostMesh m;
 };
 
-struct scg_euler
-{
-    std::unique_ptr<scg::EulerCoreBase> c;
-};
-
 using scg::guarded;
 
 namespace

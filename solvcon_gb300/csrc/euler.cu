@@ -1129,6 +1129,20 @@ public:
         }
     }
 
+    StateView state_view() override
+    {
+        StateView v{};
+        v.rec = rec[cur ^ 1].ptr;
+        v.rec_stride = RS;
+        v.neq = NEQ;
+        v.fp32 = sizeof(R) == 4;
+        v.clvol = d_clvol.ptr;
+        v.ncell = ncell;
+        v.ngstcell = ngstcell;
+        v.stream = stream;
+        return v;
+    }
+
     void cfl_range(double * out) override
     {
         double p[NEQ + 2];

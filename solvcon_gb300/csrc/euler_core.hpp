@@ -100,6 +100,20 @@ public:
     virtual void totals(double * out) = 0;
     // min and max of cflo over body cells.
     virtual void cfl_range(double * out) = 0;
+
+    // Raw device view of the newest order-0 solution (so0n rows inside the
+    // solution records), the cell volumes and the core's stream.
+    struct StateView
+    {
+        void const * rec;     // record buffer holding so0n
+        int rec_stride;       // reals per record
+        int neq;
+        bool fp32;            // records hold float instead of double
+        double const * clvol; // [ngstcell + ncell]
+        int64_t ncell, ngstcell;
+        cudaStream_t stream;
+    };
+    virtual StateView state_view() = 0;
     virtual size_t device_bytes() const = 0;
     virtual cudaStream_t get_stream() const = 0;
     // Per-launch CUDA-event timing of the fused substep kernel.
@@ -124,3 +138,9 @@ protected:
 std::unique_ptr<EulerCoreBase> make_euler_core(HostMesh const & mesh, double time_increment, int precision);
 
 } // namespace scg
+
+// The opaque handle behind scg_euler* in include/scg.h.
+struct scg_euler
+{
+    std::unique_ptr<scg::EulerCoreBase> c;
+};
