@@ -206,6 +206,81 @@ int scg_euler_profile(scg_euler * core, int on);
 int scg_euler_profile_stats(scg_euler * core, double * ms_total, int64_t * launches);
 
 /* ------------------------------------------------------------------------
+ * 1D Euler CESE core on the GPU.
+ * Replaces solvcon::onedim::Euler1DCore (cpp/solvcon/onedim/Euler1DCore.hpp:39-349)
+ * as bound by cpp/solvcon/onedim/pymod/wrap_onedim.cpp:18-162.
+ * ---------------------------------------------------------------------- */
+
+/* Array ids: 0 coord [ncoord], 1 cfl [ncoord], 2 so0 [ncoord][3],
+ * 3 so1 [ncoord][3], 4 gamma [ncoord]. */
+#define SCG_E1D_COORD 0
+#define SCG_E1D_CFL 1
+#define SCG_E1D_SO0 2
+#define SCG_E1D_SO1 3
+#define SCG_E1D_GAMMA 4
+
+/* Operation ids for scg_e1d_op (Euler1DCore.hpp:119-137, Euler1DCore.cpp:70-172). */
+#define SCG_E1D_UPDATE_CFL 0
+#define SCG_E1D_MARCH_HALF_SO0 1
+#define SCG_E1D_MARCH_HALF_SO1 2
+#define SCG_E1D_TREAT_BOUNDARY_SO0 3
+#define SCG_E1D_TREAT_BOUNDARY_SO1 4
+#define SCG_E1D_SETUP_MARCH 5
+#define SCG_E1D_MARCH_HALF1 6
+#define SCG_E1D_MARCH_HALF2 7
+
+/* Euler1DCore(ncoord, time_increment): Euler1DCore.hpp:71-75, Euler1DCore.cpp:22-35. */
+int scg_e1d_create(int64_t ncoord, double time_increment, scg_e1d ** out);
+int scg_e1d_destroy(scg_e1d * core);
+/* clone(): Euler1DCore.hpp:58-62. */
+int scg_e1d_clone(scg_e1d * core, scg_e1d ** out);
+/* ncoord and time_increment (wrap_onedim.cpp:53-54). */
+int scg_e1d_info(const scg_e1d * core, int64_t * ncoord, double * time_increment);
+/* Whole-array copies device -> host / host -> device (wrap_onedim.cpp:83-104). */
+int scg_e1d_get(scg_e1d * core, int which, double * host, int64_t count);
+int scg_e1d_set(scg_e1d * core, int which, const double * host, int64_t count);
+/* update_cfl, march_half_so0, march_half_so1_alpha<alpha>, treat_boundary_so0/so1,
+ * setup_march, march_half1_alpha<alpha>, march_half2_alpha<alpha>
+ * (wrap_onedim.cpp:107-150).  Synchronous. */
+int scg_e1d_op(scg_e1d * core, int op, int odd_plane, int alpha);
+/* march_alpha<alpha>(steps): Euler1DCore.hpp:339-349.  Asynchronous. */
+int scg_e1d_march(scg_e1d * core, int alpha, int64_t steps);
+int scg_e1d_sync(scg_e1d * core);
+int scg_e1d_stream(const scg_e1d * core, void ** out);
+
+/* ------------------------------------------------------------------------
+ * 1D spacetime scalar CESE solvers on the GPU (periodic boundary, one variable).
+ * Replaces solvcon::spacetime::LinearScalarSolver / InviscidBurgersSolver
+ * (cpp/solvcon/spacetime/kernel/linear_scalar.hpp:27-87,
+ * kernel/inviscid_burgers.hpp:30-109) and their SolverBase march
+ * (cpp/solvcon/spacetime/core.hpp:946-1036).
+ * ---------------------------------------------------------------------- */
+
+#define SCG_ST_LINEAR_SCALAR 0
+#define SCG_ST_INVISCID_BURGERS 1
+/* Array ids: 0 xcoord, 1 so0, 2 so1, 3 cfl, each [2 * ncelm + 5]. */
+#define SCG_ST_X 0
+#define SCG_ST_SO0 1
+#define SCG_ST_SO1 2
+#define SCG_ST_CFL 3
+
+/* Solver(grid, time_increment): xcoord is the grid's coordinate table
+ * (Grid::xcoord, core.cpp:52-99) of 2 * ncelm + 5 entries. */
+int scg_st_create(int kind, const double * xcoord, int64_t ncelm, double time_increment, scg_st ** out);
+int scg_st_destroy(scg_st * solver);
+/* set_time_increment (core.hpp:836). */
+int scg_st_set_time_increment(scg_st * solver, double time_increment);
+int scg_st_get(scg_st * solver, int which, double * host, int64_t count);
+int scg_st_set(scg_st * solver, int which, const double * host, int64_t count);
+/* op ids as for scg_e1d_op: 0 update_cfl, 1 march_half_so0, 2 march_half_so1_alpha,
+ * 3/4 treat_boundary_so0/so1, 5 setup_march, 6 march_half1_alpha,
+ * 7 march_half2_alpha (core.hpp:946-1025).  Synchronous. */
+int scg_st_op(scg_st * solver, int op, int odd_plane, int alpha);
+/* march_alpha<alpha>(steps): core.hpp:1027-1036.  Asynchronous. */
+int scg_st_march(scg_st * solver, int alpha, int64_t steps);
+int scg_st_sync(scg_st * solver);
+
+/* ------------------------------------------------------------------------
  * Timing and host-memory helpers (no reference counterpart: measurement
  * plumbing of this library).
  * ---------------------------------------------------------------------- */

@@ -1007,3 +1007,132 @@ void ora_e1d_march(ora_e1d * e, int alpha, int64_t steps)
         ora_e1d_march_half_so1(e, 1, alpha);
     }
 }
+
+/* ---- spacetime scalar solvers (spacetime/core.hpp:946-1036) ------------- */
+
+typedef struct
+{
+    double x, xneg, xpos, u, ux;
+} st_selm_t;
+
+static st_selm_t st_selm(const ora_st * s, int64_t ielm, int odd)
+{
+    int64_t const xi = 2 + 2 * ielm + odd; /* Grid::xindex_selm */
+    st_selm_t e = {s->xcoord[xi], s->xcoord[xi - 1], s->xcoord[xi + 1], s->so0[xi], s->so1[xi]};
+    return e;
+}
+
+static double st_xctr(const st_selm_t * e) { return (e->xneg + e->xpos) / 2; }
+
+/* LinearScalarSelm / InviscidBurgersSelm xn, xp, tp, so0p
+ * (kernel/linear_scalar.hpp:45-80, kernel/inviscid_burgers.hpp:51-100). */
+static double st_xn(const st_selm_t * e)
+{
+    double const disp = 0.5 * (e->x + e->xneg) - st_xctr(e);
+    return (e->x - e->xneg) * (e->u + disp * e->ux);
+}
+
+static double st_xp(const st_selm_t * e)
+{
+    double const disp = 0.5 * (e->x + e->xpos) - st_xctr(e);
+    return (e->xpos - e->x) * (e->u + disp * e->ux);
+}
+
+static double st_tp(const ora_st * s, const st_selm_t * e)
+{
+    double const hdt = s->dt * 0.5, qdt = s->dt * 0.25;
+    double const disp = e->x - st_xctr(e);
+    double ret;
+    if (s->kind == 0)
+    {
+        ret = e->u;
+        ret += disp * e->ux;
+        ret -= qdt * e->ux;
+    }
+    else
+    {
+        double const u2 = e->u * e->u;
+        ret = 0.5 * u2;
+        ret += disp * e->u * e->ux;
+        ret -= qdt * u2 * e->ux;
+    }
+    return hdt * ret;
+}
+
+static double st_so0p(const ora_st * s, const st_selm_t * e)
+{
+    double ret = e->u;
+    ret += (e->x - st_xctr(e)) * e->ux;
+    ret -= s->dt * 0.5 * e->ux;
+    return ret;
+}
+
+static void st_update_cfl(ora_st * s, int odd)
+{
+    for (int64_t ic = odd ? -1 : 0; ic < s->ncelm + 1; ++ic)
+    {
+        st_selm_t const e = st_selm(s, ic, odd);
+        double const dn = e.x - e.xneg, dp = e.xpos - e.x;
+        double const hdx = dn < dp ? dn : dp;
+        int64_t const xi = 2 + 2 * ic + odd;
+        s->cfl[xi] = (s->kind == 0) ? (s->dt * 0.5) / hdx : fabs(e.u) * (s->dt * 0.5) / hdx;
+    }
+}
+
+static void st_half_so0(ora_st * s, int odd)
+{
+    for (int64_t ic = odd ? -1 : 0; ic < s->ncelm; ++ic)
+    {
+        st_selm_t const xn = st_selm(s, ic, odd);
+        st_selm_t const xp = st_selm(s, ic + 1, odd);
+        double const ll = st_xp(&xn) + st_tp(s, &xn);
+        double const ur = st_xn(&xp) - st_tp(s, &xp);
+        int64_t const xt = 2 + 2 * (ic + odd) + !odd;
+        s->so0[xt] = (ll + ur) / (s->xcoord[xt + 1] - s->xcoord[xt - 1]);
+    }
+}
+
+static void st_half_so1(ora_st * s, int odd, int alpha)
+{
+    for (int64_t ic = odd ? -1 : 0; ic < s->ncelm; ++ic)
+    {
+        st_selm_t const xn = st_selm(s, ic, odd);
+        st_selm_t const xp = st_selm(s, ic + 1, odd);
+        int64_t const xt = 2 + 2 * (ic + odd) + !odd;
+        double const utp = s->so0[xt];
+        double const duxn = (utp - st_so0p(s, &xn)) / (xn.xpos - xn.x);
+        double const duxp = (st_so0p(s, &xp) - utp) / (xp.x - xp.xneg);
+        double fan = fabs(duxn), fap = fabs(duxp);
+        if (alpha == 2)
+        {
+            fan *= fan;
+            fap *= fap;
+        }
+        s->so1[xt] = (fap * duxn + fan * duxp) / (fap + fan + DBL_MIN);
+    }
+}
+
+static void st_boundary(ora_st * s, double * arr)
+{
+    int64_t const left_out = 1, left_in = 3;
+    int64_t const right_in = 2 * s->ncelm + 1, right_out = 2 * s->ncelm + 3;
+    arr[left_out] = arr[right_in];
+    arr[right_out] = arr[left_in];
+}
+
+void ora_st_march(ora_st * s, int alpha, int64_t steps)
+{
+    for (int64_t it = 0; it < steps; ++it)
+    {
+        st_half_so0(s, 0);
+        st_boundary(s, s->so0);
+        st_update_cfl(s, 1);
+        st_half_so1(s, 0, alpha);
+        st_boundary(s, s->so1);
+        st_half_so0(s, 1);
+        st_update_cfl(s, 0);
+        st_half_so1(s, 1, alpha);
+    }
+}
+
+void ora_st_setup(ora_st * s) { st_update_cfl(s, 0); }

@@ -98,6 +98,7 @@ typedef struct
     double * cfl;        /* [2 * ncelm + 5] */
 } ora_st;
 
+void ora_st_setup(ora_st * s);
 void ora_st_march(ora_st * s, int alpha, int64_t steps);
 
 #ifdef __cplusplus

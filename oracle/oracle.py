@@ -226,3 +226,35 @@ class OracleEuler1D:
 
     def march_alpha(self, alpha, steps):
         lib().ora_e1d_march(ctypes.byref(self._s), int(alpha), int(steps))
+
+
+class _OraST(ctypes.Structure):
+    _fields_ = [("ncelm", ctypes.c_int64), ("kind", ctypes.c_int32),
+                ("dt", ctypes.c_double), ("xcoord", _P), ("so0", _P),
+                ("so1", _P), ("cfl", _P)]
+
+
+class OracleSpacetime:
+    """The reference spacetime LinearScalar (kind 0) / InviscidBurgers
+    (kind 1) solver restated on the CPU; arrays are whole [2 ncelm + 5]
+    tables."""
+
+    def __init__(self, kind, xcoord, time_increment):
+        self.xcoord = np.ascontiguousarray(xcoord, dtype="float64").copy()
+        n = self.xcoord.size
+        self.ncelm = (n - 5) // 2
+        self.so0 = np.zeros(n)
+        self.so1 = np.zeros(n)
+        self.cfl = np.zeros(n)
+        self._s = _OraST(self.ncelm, int(kind), float(time_increment),
+                         self.xcoord.ctypes.data, self.so0.ctypes.data,
+                         self.so1.ctypes.data, self.cfl.ctypes.data)
+        lib().ora_st_setup.argtypes = [ctypes.c_void_p]
+        lib().ora_st_march.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_int64]
+
+    def setup_march(self):
+        lib().ora_st_setup(ctypes.byref(self._s))
+
+    def march_alpha(self, alpha, steps):
+        lib().ora_st_march(ctypes.byref(self._s), int(alpha), int(steps))

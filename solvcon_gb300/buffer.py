@@ -125,6 +125,13 @@ class SimpleArray:
         if self._on_write is not None:
             self._on_write()
 
+    def copy(self):
+        """A numpy copy of the whole buffer."""
+        return np.array(self._buf(), copy=True)
+
+    def tolist(self):
+        return self._buf().tolist()
+
     def fill(self, value):
         buf = self._buf()
         buf.fill(value)

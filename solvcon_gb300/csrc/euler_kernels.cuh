@@ -243,7 +243,13 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     R const cflc = (cflo - R(1)) * pra / (pra + Tiny<R>::CFL) + R(1);
     a.cflo[row] = cflo;
     a.cflc[row] = cflc;
-    so0n[NEQ - 1] = pra / ga1 + ke + Tiny<R>::CFL;
+    // The reference stores pra/ga1 + ke + TINY.  For pr > 0 that is exactly
+    // E + TINY (= E to working precision); re-forming it would only add a
+    // rounding error to the energy every substep, which matters in FP32.
+    if (!(pr > R(0)))
+    {
+        so0n[NEQ - 1] = pra / ga1 + ke + Tiny<R>::CFL;
+    }
     return cflc;
 }
 

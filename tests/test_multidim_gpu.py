@@ -467,3 +467,57 @@ def test_march_matches_reference_golden():
         ec.march(int(g["steps"]))
         for a in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo", "cflc"):
             assert_rel(getattr(ec, a).ndarray, g[a], 1e-10, case + " " + a)
+
+
+# -- FP32-state variants: error against the FP64 oracle -----------------------
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_fp32_state_error_against_oracle(ndim):
+    """FP32-state march (FP32 flux arithmetic with compensated face sums,
+    FP64-computed geometry) against the FP64 oracle at the workloads' CFL.
+
+    3D spherical blast (the FP32 configuration), CFL 0.7, 60 steps: relative
+    L1 <= 1e-5 per conserved variable.  2D four-quadrant state, CFL 0.8, 60
+    steps: the problem amplifies last-bit differences through the limiter's
+    min/max switches (the FP64 march itself drifts from the oracle by ~1e-6
+    relative L1 after a few hundred steps), so the bound is 2e-5 per variable
+    and 1e-5 on the whole state.  Totals: FP64 totals of the FP32 march within
+    1e-6 relative of the oracle's for mass and energy."""
+    import bench
+    from oracle import oracle as ora
+    from solvcon_gb300 import meshgen
+    if ndim == 2:
+        x, t, c = meshgen.tri_square(48, 0.2, seed=31)
+    else:
+        x, t, c = meshgen.tet_cube(8, 0.15, seed=31)
+    mesh = meshgen.build_mesh(ndim, x, t, c)
+    ng = mesh.ngstcell
+    clcnd = np.array(mesh.clcnd.ndarray)[ng:]
+    state = meshgen.quadrant_state(clcnd[:, :2], seed=31) if ndim == 2 \
+        else meshgen.blast_state(clcnd)
+    faces = np.array(mesh.bndfcs.ndarray[:, 0])
+    dt = bench.dt_for_cfl(mesh, state, faces, 0.8 if ndim == 2 else 0.7)
+    steps = 60
+    ref = ora.OracleEuler(mesh, dt)
+    ref.init_solution(GAMMA, 1.0, [0.0] * ndim, 1.0)
+    ref.so0n[ng:] = state
+    ref.add_slipwall(faces)
+    ref.call("bc_soln")
+    ref.call("bc_dsoln")
+    ref.march(steps)
+    want = np.array(ref.so0n)[ng:]
+    vol = np.array(mesh.clvol.ndarray)[ng:]
+    twant = (want * vol[:, None]).sum(axis=0)
+    per_var = 1e-5 if ndim == 3 else 2e-5
+    for prec in ("fp32", "fp32-geom64"):
+        ec = bench.setup_core(mesh, state, faces, dt, prec)
+        ec.march(steps)
+        got = np.array(ec.so0n[...])[ng:]
+        d = np.abs(got - want)
+        for k in range(ndim + 2):
+            l1 = d[:, k].sum() / np.abs(want[:, k]).sum()
+            assert l1 < per_var, (prec, k, l1)
+        assert d.sum() / np.abs(want).sum() < 1e-5
+        tgot = ec.totals()
+        for k in (0, ndim + 1):
+            assert abs(tgot[k] - twant[k]) <= 1e-6 * abs(twant[k]), (prec, k)

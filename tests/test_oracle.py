@@ -53,6 +53,36 @@ def test_oracle_reproduces_reference_sod():
         np.testing.assert_allclose(getattr(o, a), g[a], rtol=0, atol=1e-14)
 
 
+def test_oracle_spacetime_known_answers():
+    """The reference's spacetime known answers
+    (tests/test_spacetime_linear_scalar.py:106-113,
+    test_spacetime_inviscid_burgers.py:47-52) hold for the oracle."""
+    from oracle import oracle as ora
+    from solvcon_gb300.spacetime import Grid
+    res = 8
+    xcrd = np.arange(res + 1) / res * 2 * np.pi
+    grid = Grid(xcrd)
+    nstep = int(np.ceil(2 * np.pi / ((grid.xmax - grid.xmin) / grid.ncelm)))
+    dt = 2 * np.pi / nstep
+    o = ora.OracleSpacetime(0, grid.xcoord, dt)
+    o.so0[2:2 + 2 * res + 1:2] = np.sin(xcrd)
+    o.so1[2:2 + 2 * res + 1:2] = np.cos(xcrd)
+    o.setup_march()
+    o.march_alpha(2, nstep * 10)
+    np.testing.assert_allclose(o.so0[2:2 + 2 * res + 1:2], np.sin(xcrd),
+                               rtol=0, atol=1e-14)
+    np.testing.assert_allclose(o.cfl[2:2 + 2 * res + 1:2], 1.0, rtol=0,
+                               atol=1e-14)
+    b = ora.OracleSpacetime(1, grid.xcoord, dt)
+    b.so0[2:2 + 2 * res + 1:2] = np.sin(xcrd)
+    b.so1[2:2 + 2 * res + 1:2] = np.cos(xcrd)
+    b.setup_march()
+    for _ in range(nstep * 2):
+        b.march_alpha(2, 1)
+        ev = b.so0[2:2 + 2 * res + 1:2]
+        assert ev.max() <= 1 and ev.min() >= -1
+
+
 def test_oracle_free_stream_and_linear_field():
     """Known answers of the reference tests (tests/test_multidim.py:657-708):
     a uniform state is preserved exactly; a linear field's gradient is
