@@ -249,6 +249,29 @@ int scg_e1d_sync(scg_e1d * core);
 int scg_e1d_stream(const scg_e1d * core, void ** out);
 
 /* ------------------------------------------------------------------------
+ * Batched march of many independent Euler cores.  No single reference
+ * counterpart: it runs EulerCore::march (euler_march.cpp:350-359) of many
+ * cores at once, one launch per substep over a (core, row tile) work list,
+ * replayed from a CUDA graph.  The cores must share ndim and precision, must
+ * outlive the batch, and must not be used by other calls while a batch march
+ * runs.
+ * ---------------------------------------------------------------------- */
+
+typedef struct scg_batch scg_batch;
+
+/* block: 64, 128 or 256 threads per tile; persistent: grid sized to the
+ * resident capacity (blocks stride over tiles) instead of one block per tile. */
+int scg_batch_create(scg_euler * const * cores, int64_t ncore, int block, int persistent, scg_batch ** out);
+int scg_batch_destroy(scg_batch * batch);
+/* out[5] = ncore, total body cells, tiles, grid, block. */
+int scg_batch_info(const scg_batch * batch, int64_t * out);
+/* march(steps) of every core; synchronous. */
+int scg_batch_march(scg_batch * batch, int64_t steps);
+/* Device time of the last scg_batch_march's kernels (CUDA events, ms). */
+int scg_batch_last_ms(const scg_batch * batch, double * ms);
+int scg_batch_stream(const scg_batch * batch, void ** out);
+
+/* ------------------------------------------------------------------------
  * 1D spacetime scalar CESE solvers on the GPU (periodic boundary, one variable).
  * Replaces solvcon::spacetime::LinearScalarSolver / InviscidBurgersSolver
  * (cpp/solvcon/spacetime/kernel/linear_scalar.hpp:27-87,

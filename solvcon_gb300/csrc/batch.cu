@@ -1,0 +1,313 @@
+/*
+ * Batched march of many independent Euler cores in one launch per substep.
+ *
+ * Each core keeps its own device buffers.  The batch holds, per core, the
+ * kernel argument block of each of the two substeps of a step (the two
+ * differ only in which record buffer is current), and a work list of
+ * (core, row tile) pairs covering every core's body cells and ghost rows.
+ * The batch kernel walks the work list -- persistently (a grid sized to the
+ * resident capacity of the GPU, each block striding over tiles) or one block
+ * per tile -- and runs the same per-thread substep as the single-core fused
+ * kernel.  One step is two launches (a kernel boundary is the grid-wide
+ * barrier between the substeps); they are captured once into a CUDA graph and
+ * replayed.  Tile size (the block size) and the grid policy are chosen by the
+ * autotuner in solvcon_gb300/batch.py.
+ */
+
+#include "../../include/scg.h"
+#include "common.hpp"
+#include "euler_core.hpp"
+#include "euler_kernels.cuh"
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace
+{
+
+using scg::dev::MarchArgs;
+
+template <int ND, typename R, typename G, int B>
+__global__ void __launch_bounds__(B) k_fused_batch(MarchArgs<R, G> const * descs, int2 const * tiles, int ntiles)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+    {
+        int2 const tl = tiles[t];
+        MarchArgs<R, G> const a = descs[tl.x];
+        scg::dev::fused_thread<ND, R, G>(a, static_cast<int64_t>(tl.y) + threadIdx.x);
+    }
+}
+
+struct BatchBase
+{
+    virtual ~BatchBase() = default;
+    virtual void march(int64_t steps) = 0;
+    virtual void sync() = 0;
+    virtual cudaStream_t get_stream() const = 0;
+    int64_t ncore = 0, ncell = 0, ntiles = 0, grid = 0;
+    int block = 0;
+    double last_ms = 0.0; // device time of the last march's launches
+};
+
+template <int ND, typename R, typename G, int B>
+class Batch : public BatchBase
+{
+public:
+    using Args = MarchArgs<R, G>;
+
+    Batch(std::vector<scg::EulerCoreBase *> cores_in, bool persistent)
+        : cores(std::move(cores_in))
+    {
+        block = B;
+        ncore = static_cast<int64_t>(cores.size());
+        scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        scg::cuda_check(cudaEventCreate(&ev[0]), "event");
+        scg::cuda_check(cudaEventCreate(&ev[1]), "event");
+        std::vector<int2> tl;
+        for (int64_t c = 0; c < ncore; ++c)
+        {
+            auto * core = cores[static_cast<size_t>(c)];
+            int64_t const nthr = core->ncell + core->ngstcell;
+            ncell += core->ncell;
+            for (int64_t s = 0; s < nthr; s += B)
+            {
+                if (s > INT32_MAX - B)
+                {
+                    throw std::invalid_argument("EulerBatch: a core has too many rows for the work list");
+                }
+                tl.push_back(make_int2(static_cast<int>(c), static_cast<int>(s)));
+            }
+        }
+        ntiles = static_cast<int64_t>(tl.size());
+        if (ntiles > INT32_MAX)
+        {
+            throw std::invalid_argument("EulerBatch: work list too long");
+        }
+        tiles.alloc(std::max<size_t>(tl.size(), 1));
+        if (!tl.empty())
+        {
+            scg::cuda_check(cudaMemcpy(tiles.ptr, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice), "H2D");
+        }
+        for (auto & d : descs)
+        {
+            d.alloc(static_cast<size_t>(std::max<int64_t>(ncore, 1)));
+        }
+        int dev = 0, nsm = 0, occ = 0;
+        scg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        scg::cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
+        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fused_batch<ND, R, G, B>, B, 0),
+                        "occupancy");
+        int64_t const resident = static_cast<int64_t>(nsm) * std::max(occ, 1);
+        grid = persistent ? std::min<int64_t>(ntiles, resident) : ntiles;
+        grid = std::max<int64_t>(grid, 1);
+    }
+
+    ~Batch() override
+    {
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+        if (graph_exec)
+            cudaGraphExecDestroy(graph_exec);
+        if (stream)
+        {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    // Refresh both argument tables from the cores' current state.
+    void prepare()
+    {
+        std::vector<Args> h[2];
+        for (int p = 0; p < 2; ++p)
+        {
+            h[p].resize(static_cast<size_t>(ncore));
+        }
+        for (int64_t c = 0; c < ncore; ++c)
+        {
+            auto * core = cores[static_cast<size_t>(c)];
+            core->batch_begin();
+            core->fill_args(1, &h[0][static_cast<size_t>(c)], sizeof(Args));
+            core->fill_args(0, &h[1][static_cast<size_t>(c)], sizeof(Args));
+        }
+        for (int p = 0; p < 2; ++p)
+        {
+            if (ncore > 0)
+            {
+                scg::cuda_check(cudaMemcpyAsync(descs[p].ptr, h[p].data(), sizeof(Args) * h[p].size(),
+                                                cudaMemcpyHostToDevice, stream),
+                                "H2D");
+            }
+        }
+        sync();
+    }
+
+    void launch_step()
+    {
+        for (int p = 0; p < 2; ++p)
+        {
+            k_fused_batch<ND, R, G, B><<<static_cast<unsigned>(grid), B, 0, stream>>>(descs[p].ptr, tiles.ptr,
+                                                                                 static_cast<int>(ntiles));
+            scg::launched(stream, "fused_batch");
+        }
+    }
+
+    void capture()
+    {
+        cudaGraph_t g = nullptr;
+        scg::cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+        int64_t const before = scg::g_launches.load();
+        launch_step();
+        scg::g_launches.store(before);
+        scg::cuda_check(cudaStreamEndCapture(stream, &g), "EndCapture");
+        scg::cuda_check(cudaGraphInstantiate(&graph_exec, g, 0), "GraphInstantiate");
+        cudaGraphDestroy(g);
+    }
+
+    void march(int64_t steps) override
+    {
+        if (steps <= 0 || ntiles == 0)
+        {
+            return;
+        }
+        prepare();
+        if (!graph_exec)
+        {
+            capture();
+        }
+        scg::cuda_check(cudaEventRecord(ev[0], stream), "record");
+        for (int64_t s = 0; s < steps; ++s)
+        {
+            scg::cuda_check(cudaGraphLaunch(graph_exec, stream), "cudaGraphLaunch");
+            scg::g_launches.fetch_add(2, std::memory_order_relaxed);
+        }
+        scg::cuda_check(cudaEventRecord(ev[1], stream), "record");
+        sync();
+        float ms = 0.f;
+        scg::cuda_check(cudaEventElapsedTime(&ms, ev[0], ev[1]), "elapsed");
+        last_ms = ms;
+        for (auto * core : cores)
+        {
+            core->batch_end(steps);
+        }
+    }
+
+    void sync() override { scg::cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+    cudaStream_t get_stream() const override { return stream; }
+
+private:
+    std::vector<scg::EulerCoreBase *> cores;
+    scg::DevBuf<Args> descs[2];
+    scg::DevBuf<int2> tiles;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+template <int ND, typename R, typename G>
+std::unique_ptr<BatchBase> make_for_block(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)
+{
+    switch (block)
+    {
+    case 64: return std::make_unique<Batch<ND, R, G, 64>>(std::move(cores), persistent);
+    case 128: return std::make_unique<Batch<ND, R, G, 128>>(std::move(cores), persistent);
+    case 256: return std::make_unique<Batch<ND, R, G, 256>>(std::move(cores), persistent);
+    default: throw std::invalid_argument("EulerBatch: block must be 64, 128 or 256");
+    }
+}
+
+std::unique_ptr<BatchBase> make_batch(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)
+{
+    if (cores.empty())
+    {
+        throw std::invalid_argument("EulerBatch: no cores");
+    }
+    int const nd = cores[0]->ndim;
+    int const prec = cores[0]->precision;
+    for (auto * c : cores)
+    {
+        if (c->ndim != nd || c->precision != prec)
+        {
+            throw std::invalid_argument("EulerBatch: every core must have the same ndim and precision");
+        }
+    }
+    if (nd == 2)
+    {
+        if (prec == scg::PREC_FP64)
+            return make_for_block<2, double, double>(std::move(cores), block, persistent);
+        if (prec == scg::PREC_FP32_GEOM64)
+            return make_for_block<2, float, double>(std::move(cores), block, persistent);
+        return make_for_block<2, float, float>(std::move(cores), block, persistent);
+    }
+    if (prec == scg::PREC_FP64)
+        return make_for_block<3, double, double>(std::move(cores), block, persistent);
+    if (prec == scg::PREC_FP32_GEOM64)
+        return make_for_block<3, float, double>(std::move(cores), block, persistent);
+    return make_for_block<3, float, float>(std::move(cores), block, persistent);
+}
+
+} // namespace
+
+struct scg_batch
+{
+    std::unique_ptr<BatchBase> b;
+};
+
+extern "C"
+{
+
+int scg_batch_create(scg_euler * const * cores, int64_t ncore, int block, int persistent, scg_batch ** out)
+{
+    return scg::guarded([&] {
+        std::vector<scg::EulerCoreBase *> v;
+        for (int64_t i = 0; i < ncore; ++i)
+        {
+            if (!cores[i] || !cores[i]->c)
+            {
+                throw std::invalid_argument("EulerBatch: null core handle");
+            }
+            v.push_back(cores[i]->c.get());
+        }
+        auto h = std::make_unique<scg_batch>();
+        h->b = make_batch(std::move(v), block, persistent != 0);
+        *out = h.release();
+    });
+}
+
+int scg_batch_destroy(scg_batch * batch)
+{
+    return scg::guarded([&] { delete batch; });
+}
+
+int scg_batch_info(const scg_batch * batch, int64_t * out)
+{
+    return scg::guarded([&] {
+        out[0] = batch->b->ncore;
+        out[1] = batch->b->ncell;
+        out[2] = batch->b->ntiles;
+        out[3] = batch->b->grid;
+        out[4] = batch->b->block;
+    });
+}
+
+int scg_batch_last_ms(const scg_batch * batch, double * ms)
+{
+    return scg::guarded([&] { *ms = batch->b->last_ms; });
+}
+
+int scg_batch_march(scg_batch * batch, int64_t steps)
+{
+    return scg::guarded([&] {
+        if (steps < 0)
+            throw std::invalid_argument("EulerBatch::march: steps must be >= 0");
+        batch->b->march(steps);
+    });
+}
+
+int scg_batch_stream(const scg_batch * batch, void ** out)
+{
+    return scg::guarded([&] { *out = batch->b->get_stream(); });
+}
+
+} // extern "C"

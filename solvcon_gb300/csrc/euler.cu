@@ -1129,6 +1129,47 @@ public:
         }
     }
 
+    void batch_begin() override
+    {
+        upload_bc();
+        // Exactly what the first substep of march() does before its fused
+        // kernel, minus the buffer swap: so0t of the state in rec[cur ^ 1].
+        if (!(next_valid && next_buf == (cur ^ 1)) && nrow > 0)
+        {
+            k_solt_rows<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_gamma.ptr, nrow);
+            launched(stream, "calc_solt");
+            next_valid = true;
+            next_buf = cur ^ 1;
+        }
+        sync();
+    }
+
+    void fill_args(int offset, void * out, size_t size) override
+    {
+        if (size != sizeof(MarchArgs<R, G>))
+        {
+            throw std::invalid_argument("EulerCore: argument block size mismatch");
+        }
+        int const saved = cur;
+        cur ^= (offset & 1);
+        MarchArgs<R, G> const a = args();
+        cur = saved;
+        std::memcpy(out, &a, sizeof(a));
+    }
+
+    void batch_end(int64_t steps) override
+    {
+        if (steps > 0)
+        {
+            // Two substeps per step leave cur unchanged; the second substep's
+            // current buffer holds the logical so0t and the fused kernel left
+            // the next so0t in the other buffer.
+            tbuf = cur;
+            next_valid = true;
+            next_buf = cur ^ 1;
+        }
+    }
+
     StateView state_view() override
     {
         StateView v{};

@@ -114,6 +114,16 @@ public:
         cudaStream_t stream;
     };
     virtual StateView state_view() = 0;
+
+    // Batched march support (batch.cu).  batch_begin() leaves the core ready
+    // for fused substeps run by someone else: boundary tables uploaded and the
+    // next substep's so0t computed.  fill_args() writes the kernel argument
+    // block (dev::MarchArgs<R, G>) of the substep whose current buffer is
+    // cur ^ offset into out (size bytes).  batch_end(steps) records that
+    // `steps` full steps ran.
+    virtual void batch_begin() = 0;
+    virtual void fill_args(int offset, void * out, size_t size) = 0;
+    virtual void batch_end(int64_t steps) = 0;
     virtual size_t device_bytes() const = 0;
     virtual cudaStream_t get_stream() const = 0;
     // Per-launch CUDA-event timing of the fused substep kernel.

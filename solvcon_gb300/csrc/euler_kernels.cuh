@@ -648,10 +648,11 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     store_rec<ND, R>(a.nxt + row * D::RS, so0n, so0t, so1n);
 }
 
+// The work of thread t of one substep: body cell t for t < ncell, ghost row
+// t - ncell after that.
 template <int ND, typename R, typename G>
-__global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
+__device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t t)
 {
-    int64_t const t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t < a.ncell)
     {
         int const ct = a.ctype[t];
@@ -688,6 +689,12 @@ __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
             store_rec<ND, R>(a.nxt + g * Dim<ND>::RS, rec, tt, rec + 2 * NEQ);
         }
     }
+}
+
+template <int ND, typename R, typename G>
+__global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
+{
+    fused_thread<ND, R, G>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
 } // namespace dev
