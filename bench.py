@@ -462,6 +462,64 @@ def run_batch(args, world, rank, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args, world, rank, dist):
+    """Config 5: Poisson arrivals of mixed 1D tubes (30%) and 2D meshes
+    (70%, the batched workload's distribution), 200-2000 steps each, served
+    with continuous batching under a 120 GB HBM budget; p50/p99 latency and
+    aggregate cell-steps/s per arrival rate, against each request marched
+    alone with the plain FP64 march."""
+    from solvcon_gb300 import serving
+    nreq = args.nreq
+    data = batch_meshes(args.nmesh, seed=4242 + 1000 * rank)
+    srv = serving.Server(hbm_budget=120 * 2 ** 30, max_chunk=64,
+                         precision=args.precision or "fp32")
+    for k, (m, s, f, g) in enumerate(data):
+        srv.add_mesh(k, m, s, f, g, dt_for_cfl_g(m, s, 0.8, g))
+    keys = list(range(len(data)))
+    # Warm-up pass: creates every slot and captures the graphs.
+    srv.run(serving.make_requests(nreq, 1e6, keys, seed=7))
+    rates = [float(r) for r in args.rates.split(",")]
+    per_rate = []
+    for rate in rates:
+        reqs = serving.make_requests(nreq, rate, keys, seed=7)
+        done = srv.run(reqs)
+        st = serving.stats(done, srv.makespan)
+        st["rate_req_per_s"] = rate
+        st["rejected"] = len(srv.rejected)
+        st["peak_resident"] = srv.peak_resident
+        per_rate.append(st)
+    # Each request alone with the plain FP64 march (the same request set).
+    reqs = serving.make_requests(nreq, 1.0, keys, seed=7)
+    alone_s = 0.0
+    work = 0
+    for r in reqs:
+        _, secs = serving.alone(srv, r, "fp64")
+        alone_s += secs
+        cells = srv.meshes[r.mesh_key].mesh.ncell if r.kind == "2d" \
+            else r.ncoord
+        work += cells * r.steps
+    alone_rate = work / alone_s
+    best = max(per_rate, key=lambda s: s["cell_steps_per_s"])
+    line = {
+        "metric": "cell-steps/s", "value": best["cell_steps_per_s"],
+        "unit": "cell-steps/s", "n_gpus": world, "steps": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (2D) / f64 (1D)", "data": "synthetic",
+        "config": {"workload": "serve (%d requests per rate: 30%% 1D Sod-type "
+                               "tubes of 1k-100k points, 70%% 2D meshes of "
+                               "the batched distribution, 200-2000 steps; "
+                               "HBM budget 120 GB; continuous batching)"
+                               % nreq, "rates": rates},
+        "per_rate": per_rate,
+        "baseline_alone_plain_fp64": {"value": alone_rate,
+                                      "unit": "cell-steps/s",
+                                      "seconds": alone_s},
+        "speedup_vs_alone_fp64": best["cell_steps_per_s"] / alone_rate,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def _desc(w):
     if w["ndim"] == 2:
         return ("2D Euler, unit square %dx%d quads x 2 triangles = %d cells, "
@@ -480,7 +538,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tri2d",
-                    choices=sorted(WORKLOADS) + ["batch"])
+                    choices=sorted(WORKLOADS) + ["batch", "serve"])
     ap.add_argument("--precision", default=None,
                     choices=["fp64", "fp32", "fp32-geom64"])
     ap.add_argument("--nside", type=int, default=None)
@@ -488,18 +546,23 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
-    ap.add_argument("--nmesh", type=int, default=512)
+    ap.add_argument("--nmesh", type=int, default=None)
+    ap.add_argument("--nreq", type=int, default=64)
+    ap.add_argument("--rates", default="50,200,1000,2000")
     args = ap.parse_args()
+    if args.nmesh is None:
+        args.nmesh = 512 if args.workload == "batch" else 64
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         return
-    if args.workload == "batch":
+    if args.workload in ("batch", "serve"):
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
         import solvcon_gb300  # noqa: F401
-        run_batch(args, world, rank, dist)
+        (run_batch if args.workload == "batch" else run_serve)(
+            args, world, rank, dist)
         if dist is not None:
             dist.destroy_process_group()
         return
