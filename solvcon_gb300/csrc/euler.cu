@@ -48,13 +48,19 @@ __global__ void k_solt_rows(R * rec, R const * gamma, int64_t nrow)
     {
         return;
     }
-    R v[2 * NEQ + NEQ * ND];
-    load_rec<ND, R>(rec + r * Dim<ND>::RS, v);
+    using RC = Rec<ND, R>;
+    R v[RC::NUSED];
+    load_rec<ND, R>(rec + r * RC::RS, v);
     R t[NEQ];
-    solt_row<ND, R>(v, v + 2 * NEQ, gamma[r], t);
+    Prim<ND, R> const q(v, gamma[r]);
+    solt_prim<ND, R>(q, v, v + 2 * NEQ, t);
     for (int i = 0; i < NEQ; ++i)
     {
-        rec[r * Dim<ND>::RS + NEQ + i] = t[i];
+        rec[r * RC::RS + NEQ + i] = t[i];
+    }
+    if constexpr (RC::PRIM)
+    {
+        q.cache(rec + r * RC::RS + RC::OP);
     }
 }
 
@@ -68,7 +74,7 @@ __global__ void k_copy_field(R const * src, R * dst, int64_t nrow, int off, int 
     }
     for (int k = 0; k < width; ++k)
     {
-        dst[r * Dim<ND>::RS + off + k] = src[r * Dim<ND>::RS + off + k];
+        dst[r * Rec<ND, R>::RS + off + k] = src[r * Rec<ND, R>::RS + off + k];
     }
 }
 
@@ -100,7 +106,7 @@ __global__ void k_soln(MarchArgs<R, G> a)
         default: soln_cell<8, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
         }
     }
-    R * out = a.nxt + (icl + a.ngst) * Dim<ND>::RS;
+    R * out = a.nxt + (icl + a.ngst) * Rec<ND, R>::RS;
     for (int i = 0; i < NEQ; ++i)
     {
         out[i] = so0n[i];
@@ -117,13 +123,14 @@ __global__ void k_cfl(MarchArgs<R, G> a)
         return;
     }
     int64_t const row = icl + a.ngst;
-    R * out = a.nxt + row * Dim<ND>::RS;
+    R * out = a.nxt + row * Rec<ND, R>::RS;
     R s[NEQ];
     for (int i = 0; i < NEQ; ++i)
     {
         s[i] = out[i];
     }
-    cfl_cell<ND, R, G>(a, icl, row, s);
+    R rinv;
+    cfl_cell<ND, R, G>(a, icl, row, s, rinv);
     out[NEQ - 1] = s[NEQ - 1];
 }
 
@@ -137,7 +144,7 @@ __global__ void k_dsoln(MarchArgs<R, G> a)
         return;
     }
     int64_t const row = icl + a.ngst;
-    R * out = a.nxt + row * Dim<ND>::RS;
+    R * out = a.nxt + row * Rec<ND, R>::RS;
     R s[NEQ];
     for (int i = 0; i < NEQ; ++i)
     {
@@ -179,14 +186,14 @@ __global__ void k_bc0(MarchArgs<R, G> a, int32_t const * gint)
     {
         return;
     }
-    R const * in = a.nxt + static_cast<int64_t>(gint[g]) * Dim<ND>::RS;
+    R const * in = a.nxt + static_cast<int64_t>(gint[g]) * Rec<ND, R>::RS;
     R s[NEQ], o[NEQ];
     for (int i = 0; i < NEQ; ++i)
     {
         s[i] = in[i];
     }
     bc0_ghost<ND, R>(a.gkind[g], a.gnml + g * ND, a.gval + g * NEQ, s, o);
-    R * out = a.nxt + g * Dim<ND>::RS;
+    R * out = a.nxt + g * Rec<ND, R>::RS;
     for (int i = 0; i < NEQ; ++i)
     {
         out[i] = o[i];
@@ -203,14 +210,14 @@ __global__ void k_bc1(MarchArgs<R, G> a, int32_t const * gint)
     {
         return;
     }
-    R const * in = a.cur + static_cast<int64_t>(gint[g]) * Dim<ND>::RS + 2 * NEQ;
+    R const * in = a.cur + static_cast<int64_t>(gint[g]) * Rec<ND, R>::RS + 2 * NEQ;
     R s[NEQ * ND], o[NEQ * ND];
     for (int i = 0; i < NEQ * ND; ++i)
     {
         s[i] = in[i];
     }
     bc1_ghost<ND, R>(a.gkind[g], a.gnml + g * ND, s, o);
-    R * out = a.nxt + g * Dim<ND>::RS + 2 * NEQ;
+    R * out = a.nxt + g * Rec<ND, R>::RS + 2 * NEQ;
     for (int i = 0; i < NEQ * ND; ++i)
     {
         out[i] = o[i];
@@ -231,7 +238,7 @@ __global__ void k_init(R * nxt, R * gamma, int64_t ngst, int64_t nrow, double ga
     gamma[r] = R(ga);
     if (r >= ngst)
     {
-        R * o = nxt + r * Dim<ND>::RS;
+        R * o = nxt + r * Rec<ND, R>::RS;
         o[0] = R(rho);
         o[1] = R(m0);
         o[2] = R(m1);
@@ -254,7 +261,7 @@ __global__ void k_get_field(R const * rec, double * out, int64_t nrow, int off, 
     }
     for (int k = 0; k < width; ++k)
     {
-        out[r * width + k] = double(rec[r * Dim<ND>::RS + off + k]);
+        out[r * width + k] = double(rec[r * Rec<ND, R>::RS + off + k]);
     }
 }
 
@@ -268,7 +275,7 @@ __global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, i
     }
     for (int k = 0; k < width; ++k)
     {
-        rec[r * Dim<ND>::RS + off + k] = R(in[r * width + k]);
+        rec[r * Rec<ND, R>::RS + off + k] = R(in[r * width + k]);
     }
 }
 
@@ -314,7 +321,7 @@ __global__ void k_totals(R const * nxt, double const * clvol, R const * cflo, in
         double const v = clvol[row];
         for (int i = 0; i < NEQ; ++i)
         {
-            double const y = double(nxt[row * Dim<ND>::RS + i]) * v - c[i];
+            double const y = double(nxt[row * Rec<ND, R>::RS + i]) * v - c[i];
             double const t = s[i] + y;
             c[i] = (t - s[i]) - y;
             s[i] = t;
@@ -500,7 +507,7 @@ class EulerCoreImpl : public EulerCoreBase
 {
 public:
     static constexpr int NEQ = ND + 2;
-    static constexpr int RS = Dim<ND>::RS;
+    static constexpr int RS = Rec<ND, R>::RS;
     static constexpr int KF = Dim<ND>::KF;
 
     EulerCoreImpl(HostMesh const & mesh, double dt, int prec)
@@ -554,6 +561,7 @@ public:
                                             std::to_string(t) + " unsupported in " + std::to_string(ND) + "D");
             }
             nslot = std::max(nslot, static_cast<int>(mesh.clfcs(icl, 0)));
+            single_ct = (icl == 0 || single_ct == t) ? t : -1;
         }
 
         // Solution state.
@@ -1055,7 +1063,7 @@ public:
                 cuda_check(cudaEventCreate(&e1), "event");
                 cuda_check(cudaEventRecord(e0, stream), "record");
             }
-            k_fused<ND, R, G><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            launch_fused();
             launched(stream, "fused_substep");
             if (profiling)
             {
@@ -1064,6 +1072,21 @@ public:
             }
             next_valid = true;
             next_buf = cur ^ 1;
+        }
+    }
+
+    // The fused kernel specialised to the mesh's cell type when it has only
+    // triangles or only tetrahedra (the simplex paths), else the generic one.
+    void launch_fused()
+    {
+        constexpr int SIMPLEX = (ND == 2) ? CT_TRIANGLE : CT_TET;
+        if (single_ct == SIMPLEX)
+        {
+            k_fused<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+        }
+        else
+        {
+            k_fused<ND, R, G><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
         }
     }
 
@@ -1224,6 +1247,7 @@ private:
 
     int64_t nrow = 0;
     int nslot = 0;
+    int single_ct = -1; // the cell type if all cells share one, else -1
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     MeshView mv{};
@@ -1247,7 +1271,7 @@ private:
 
     int cur = 0;           // index of the current (so0c/so1c) record buffer
     int tbuf = 0;          // buffer holding the logical so0t
-    bool next_valid = false; // rec[next_buf].so0t == calc_solt of rec[next_buf]
+    bool next_valid = false; // rec[next_buf].so0t (and its primitive cache) == calc_solt of rec[next_buf]
     int next_buf = 1;
 };
 

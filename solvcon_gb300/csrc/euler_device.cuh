@@ -29,7 +29,12 @@
  * Results equal the reference's up to floating-point round-off.
  *
  * Storage (one record per mesh row, ghost rows first, row = icl + ngstcell):
- *   record[row] = { so0[NEQ], so0t[NEQ], so1[NEQ][ND] } padded to RS reals.
+ *   record[row] = { so0[NEQ], so0t[NEQ], so1[NEQ][ND], prim } padded to RS
+ * reals, where prim (FP64 records only) caches the primitive variables of so0
+ * (1/rho, v, p, E + p, |v|^2).  It is written with so0t, by the same thread
+ * and from the same state, so it is valid exactly when so0t is; the fused
+ * march then reads a neighbour's primitives instead of re-deriving them for
+ * every face (a division and about twenty FP64 operations each).
  */
 
 #include <cstdint>
@@ -57,6 +62,22 @@ struct Dim
     static constexpr int KF = K_R + ND;
     // Cell geometry components: 1/cevol[0], hdt/dist.
     static constexpr int KC = 2;
+};
+
+// Record layout per dimension and state precision.
+template <int ND, typename R>
+struct Rec
+{
+    static constexpr int NEQ = ND + 2;
+    static constexpr int NUSED = 2 * NEQ + NEQ * ND; // so0, so0t, so1: 16 / 25
+    // Primitive cache (FP64 only: the FP64 march is bound by the FP64 pipe,
+    // the FP32 march by memory, where the extra bytes would cost more).
+    static constexpr bool PRIM = sizeof(R) == 8;
+    static constexpr int OP = NUSED;    // cache offset: r, v[ND], p, h, vsq
+    static constexpr int NPRIM = ND + 4;
+    static constexpr int NLOAD = PRIM ? NUSED + NPRIM : NUSED;
+    static constexpr int RS = (ND == 2) ? (PRIM ? 24 : 16) : 32;
+    static_assert(NLOAD <= RS, "record overflow");
 };
 
 // Small constants of the reference, with FP32-safe floors.  The FP64 values
@@ -121,10 +142,13 @@ struct Prim
     R ga1;   // gamma - 1
     R vsq;   // |v|^2
 
-    __device__ __forceinline__ Prim(R const * u, R ga)
+    __device__ __forceinline__ Prim(R const * u, R ga) : Prim(u, ga, R(1) / (u[0] + Tiny<R>::JAC)) {}
+
+    // With 1/(rho + TINY) already at hand.
+    __device__ __forceinline__ Prim(R const * u, R ga, R rinv)
     {
         constexpr int NEQ = ND + 2;
-        r = R(1) / (u[0] + Tiny<R>::JAC);
+        r = rinv;
         R ke2 = R(0);
 #pragma unroll
         for (int d = 0; d < ND; ++d)
@@ -136,6 +160,38 @@ struct Prim
         ga1 = ga - R(1);
         p = ga1 * (u[NEQ - 1] - R(0.5) * ke2);
         h = u[NEQ - 1] + p;
+    }
+
+    Prim() = default;
+
+    // From a record's primitive cache (see Rec).
+    __device__ __forceinline__ static Prim cached(R const * c, R ga)
+    {
+        Prim q;
+        q.r = c[0];
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            q.v[d] = c[1 + d];
+        }
+        q.p = c[1 + ND];
+        q.h = c[2 + ND];
+        q.vsq = c[3 + ND];
+        q.ga1 = ga - R(1);
+        return q;
+    }
+
+    __device__ __forceinline__ void cache(R * c) const
+    {
+        c[0] = r;
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            c[1 + d] = v[d];
+        }
+        c[1 + ND] = p;
+        c[2 + ND] = h;
+        c[3 + ND] = vsq;
     }
 };
 
@@ -192,12 +248,12 @@ __device__ __forceinline__ void jvp_sum(Prim<ND, R> const & q, R const * u, R co
     }
 }
 
-// so0t = -(J . so1) for one row (euler_march.cpp:160-191).
+// so0t = -(J . so1) for one row (euler_march.cpp:160-191), from the row's
+// primitives q.
 template <int ND, typename R>
-__device__ __forceinline__ void solt_row(R const * u, R const * g, R ga, R * t)
+__device__ __forceinline__ void solt_prim(Prim<ND, R> const & q, R const * u, R const * g, R * t)
 {
     constexpr int NEQ = ND + 2;
-    Prim<ND, R> const q(u, ga);
     R o[NEQ];
 #pragma unroll
     for (int i = 0; i < NEQ; ++i)
@@ -210,6 +266,12 @@ __device__ __forceinline__ void solt_row(R const * u, R const * g, R ga, R * t)
     {
         t[i] = -o[i];
     }
+}
+
+template <int ND, typename R>
+__device__ __forceinline__ void solt_row(R const * u, R const * g, R ga, R * t)
+{
+    solt_prim<ND, R>(Prim<ND, R>(u, ga), u, g, t);
 }
 
 // Fundamental gradient element tables (1-based in GradientElement.cpp:

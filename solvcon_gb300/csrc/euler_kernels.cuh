@@ -21,11 +21,10 @@ __device__ __forceinline__ T ldg(T const * p)
     return __ldg(p);
 }
 
-// Load the used part of a record (so0, so0t, so1).
-template <int ND, typename R>
+// Load the first N reals of a record (default: so0, so0t, so1).
+template <int ND, typename R, int N = Rec<ND, R>::NUSED>
 __device__ __forceinline__ void load_rec(R const * base, R * out)
 {
-    constexpr int N = 2 * (ND + 2) + (ND + 2) * ND; // 16 (2D) or 25 (3D)
     if constexpr (sizeof(R) == 8)
     {
         double2 const * p = reinterpret_cast<double2 const *>(base);
@@ -61,12 +60,14 @@ __device__ __forceinline__ void load_rec(R const * base, R * out)
     }
 }
 
-// Store the used part of a record (so0, so0t, so1).
+// Store a record: so0, so0t, so1 and (FP64) the primitive cache of so0.
 template <int ND, typename R>
-__device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0t, R const * so1)
+__device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0t, R const * so1,
+                                          Prim<ND, R> const & q)
 {
     constexpr int NEQ = ND + 2;
-    constexpr int N = 2 * NEQ + NEQ * ND;
+    using RC = Rec<ND, R>;
+    constexpr int N = RC::NLOAD;
     R v[N];
 #pragma unroll
     for (int i = 0; i < NEQ; ++i)
@@ -78,6 +79,14 @@ __device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0
     for (int i = 0; i < NEQ * ND; ++i)
     {
         v[2 * NEQ + i] = so1[i];
+    }
+    if constexpr (RC::PRIM)
+    {
+        q.cache(v + RC::OP);
+    }
+    else
+    {
+        (void)q;
     }
     if constexpr (sizeof(R) == 8)
     {
@@ -121,20 +130,25 @@ __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t
 // element's solution deltas that need only neighbour data:
 //   alpha = so0c + hdt so0t + R . so1c,   beta = Q . so1c
 // so that calc_dsoln needs no second gather.
-template <int CT, typename R, typename G, bool AB>
+//
+// With CACHE set (the fused march, where every record's primitive cache is
+// valid) a neighbour's primitives come from its record.
+template <int CT, typename R, typename G, bool AB, bool CACHE = false>
 __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n, R * alpha, R * beta)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
     constexpr int NFC = CellT<CT>::NFC;
     using D = Dim<ND>;
+    using RC = Rec<ND, R>;
+    constexpr bool USE = CACHE && RC::PRIM;
     Acc<R> acc[NEQ];
 #pragma unroll
     for (int f = 0; f < NFC; ++f)
     {
         int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
-        R rec[2 * NEQ + NEQ * ND];
-        load_rec<ND, R>(a.cur + jr * D::RS, rec);
+        R rec[USE ? RC::NLOAD : RC::NUSED];
+        load_rec<ND, R, USE ? RC::NLOAD : RC::NUSED>(a.cur + jr * RC::RS, rec);
         R const * u = rec;
         R const * t = rec + NEQ;
         R const * g = rec + 2 * NEQ;
@@ -178,7 +192,15 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
                 w[i * ND + d] = s;
             }
         }
-        Prim<ND, R> const q(u, ga);
+        Prim<ND, R> q;
+        if constexpr (USE)
+        {
+            q = Prim<ND, R>::cached(rec + RC::OP, ga);
+        }
+        else
+        {
+            q = Prim<ND, R>(u, ga);
+        }
         R fl[NEQ];
         flux_dot<ND, R>(q, u, nh, fl);
         jvp_sum<ND, R>(q, u, w, fl);
@@ -221,24 +243,29 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
 }
 
 // calc_cfl for one body cell (euler_solution.cpp:240-294): original and
-// clamped CFL, and the energy rewritten from the non-negative pressure.
+// clamped CFL, and the energy rewritten from the non-negative pressure.  The
+// reference's three divisions by rho use one reciprocal 1/(rho + TINY) (the
+// floor changes nothing unless rho is below 1e-44 in FP64, 1e-23 in FP32,
+// where the reference itself produces inf); it is returned in rinv for the
+// primitives of the same state.
 template <int ND, typename R, typename G>
-__device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, int64_t row, R * so0n)
+__device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, int64_t row, R * so0n, R & rinv)
 {
     constexpr int NEQ = ND + 2;
     R const ga = ldg(a.gamma + row);
     R const ga1 = ga - R(1);
-    R const rho = so0n[0];
+    R const ri = R(1) / (so0n[0] + Tiny<R>::JAC);
+    rinv = ri;
     R momsq = R(0);
 #pragma unroll
     for (int d = 0; d < ND; ++d)
     {
         momsq += so0n[1 + d] * so0n[1 + d];
     }
-    R const ke = momsq / (R(2) * rho);
+    R const ke = R(0.5) * momsq * ri;
     R const pr = ga1 * (so0n[NEQ - 1] - ke);
     R const pra = (pr + fabs(pr)) / R(2);
-    R const wspd = sqr_t(ga * pra / rho) + sqr_t(momsq) / rho;
+    R const wspd = sqr_t(ga * pra * ri) + sqr_t(momsq) * ri;
     R const cflo = wspd * R(ldg(a.cgeo + 1 * a.ncell + icl));
     R const cflc = (cflo - R(1)) * pra / (pra + Tiny<R>::CFL) + R(1);
     a.cflo[row] = cflo;
@@ -350,8 +377,8 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
         for (int f = 0; f < NFC; ++f)
         {
             int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
-            R rec[2 * NEQ + NEQ * ND];
-            load_rec<ND, R>(a.cur + jr * D::RS, rec);
+            R rec[Rec<ND, R>::NUSED];
+            load_rec<ND, R>(a.cur + jr * Rec<ND, R>::RS, rec);
             R jd[ND];
 #pragma unroll
             for (int d = 0; d < ND; ++d)
@@ -373,8 +400,12 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     }
 
     // Rows of each element's inverse displacement matrix (prescaled by
-    // 1/det): grad = sum_v uf[v] * C[k][v].
-    R C[NFGE][ND][ND];
+    // 1/det): grad = sum_v uf[v] * C[k][v].  In FP64 the NFGE reciprocals
+    // come from one division by the product of the determinants (prefix
+    // products, then peeled off backwards); in FP32 that product could
+    // underflow, so each element divides.
+    R dets[NFGE];
+    R bcx[NFGE][ND == 3 ? 3 : 1]; // 3D: rb x rc, the first row of the adjugate
 #pragma unroll
     for (int k = 0; k < NFGE; ++k)
     {
@@ -382,7 +413,53 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
         R const * rb = idis[CellT<CT>::fge(k, 1)];
         if constexpr (ND == 2)
         {
-            R const inv = R(1) / (ra[0] * rb[1] - ra[1] * rb[0]);
+            dets[k] = ra[0] * rb[1] - ra[1] * rb[0];
+        }
+        else
+        {
+            R const * rc = idis[CellT<CT>::fge(k, ND - 1)];
+            bcx[k][0] = rb[1] * rc[2] - rb[2] * rc[1];
+            bcx[k][1] = rb[2] * rc[0] - rb[0] * rc[2];
+            bcx[k][2] = rb[0] * rc[1] - rb[1] * rc[0];
+            dets[k] = ra[0] * bcx[k][0] + ra[1] * bcx[k][1] + ra[2] * bcx[k][2];
+        }
+    }
+    R invs[NFGE];
+    if constexpr (sizeof(R) == 8)
+    {
+        R pre[NFGE];
+        pre[0] = dets[0];
+#pragma unroll
+        for (int k = 1; k < NFGE; ++k)
+        {
+            pre[k] = pre[k - 1] * dets[k];
+        }
+        R inv = R(1) / pre[NFGE - 1];
+#pragma unroll
+        for (int k = NFGE - 1; k > 0; --k)
+        {
+            invs[k] = inv * pre[k - 1];
+            inv *= dets[k];
+        }
+        invs[0] = inv;
+    }
+    else
+    {
+#pragma unroll
+        for (int k = 0; k < NFGE; ++k)
+        {
+            invs[k] = R(1) / dets[k];
+        }
+    }
+    R C[NFGE][ND][ND];
+#pragma unroll
+    for (int k = 0; k < NFGE; ++k)
+    {
+        R const * ra = idis[CellT<CT>::fge(k, 0)];
+        R const * rb = idis[CellT<CT>::fge(k, 1)];
+        R const inv = invs[k];
+        if constexpr (ND == 2)
+        {
             C[k][0][0] = rb[1] * inv;
             C[k][0][1] = -rb[0] * inv;
             C[k][1][0] = -ra[1] * inv;
@@ -391,13 +468,9 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
         else
         {
             R const * rc = idis[CellT<CT>::fge(k, ND - 1)];
-            R const bc0 = rb[1] * rc[2] - rb[2] * rc[1];
-            R const bc1 = rb[2] * rc[0] - rb[0] * rc[2];
-            R const bc2 = rb[0] * rc[1] - rb[1] * rc[0];
-            R const inv = R(1) / (ra[0] * bc0 + ra[1] * bc1 + ra[2] * bc2);
-            C[k][0][0] = bc0 * inv;
-            C[k][0][1] = bc1 * inv;
-            C[k][0][2] = bc2 * inv;
+            C[k][0][0] = bcx[k][0] * inv;
+            C[k][0][1] = bcx[k][1] * inv;
+            C[k][0][2] = bcx[k][2] * inv;
             C[k][1][0] = (rc[1] * ra[2] - rc[2] * ra[1]) * inv;
             C[k][1][1] = (rc[2] * ra[0] - rc[0] * ra[2]) * inv;
             C[k][1][2] = (rc[0] * ra[1] - rc[1] * ra[0]) * inv;
@@ -444,8 +517,15 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             wmax = fmax(wmax, wgt[k]);
             wmin = fmin(wmin, wgt[k]);
         }
-        // W-3/4 cap.
-        R const sm = fmin((R(1) - ofg1) / (wmax + Tiny<R>::AZ), -ofg1 / (wmin - Tiny<R>::AZ));
+        // W-3/4 cap: sm = min(A / a1, B / a2) with A = 1 - 1/n > 0,
+        // a1 = wmax + TINY > 0, B = -1/n < 0, a2 = wmin - TINY < 0.  Both
+        // quotients are positive, and A / a1 <= B / a2 exactly when
+        // A a2 >= B a1, so the smaller one is chosen first and one division
+        // is taken instead of two.
+        R const a1 = wmax + Tiny<R>::AZ;
+        R const a2 = wmin - Tiny<R>::AZ;
+        bool const first = (R(1) - ofg1) * a2 >= -ofg1 * a1;
+        R const sm = (first ? R(1) - ofg1 : -ofg1) / (first ? a1 : a2);
         R const sig = fmin(sm, sgm0);
         if (sm < sgm0)
         {
@@ -610,14 +690,17 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
     constexpr int NFC = CellT<CT>::NFC;
-    constexpr bool AB = CellT<CT>::SIMPLEX;
-    using D = Dim<ND>;
+    // Simplices carry calc_dsoln's neighbour terms over from calc_soln's
+    // gather in FP32 (memory-bound: no second gather); in FP64 (FP64-pipe
+    // bound) calc_dsoln gathers again, which takes fewer FP64 operations
+    // and registers, and the second gather hits in cache.
+    constexpr bool AB = CellT<CT>::SIMPLEX && !Rec<ND, R>::PRIM;
     int64_t const row = icl + a.ngst;
 
     R so0n[NEQ];
     R alpha[AB ? NFC * NEQ : 1];
     R beta[AB ? NFC * NEQ : 1];
-    soln_cell<CT, R, G, AB>(a, icl, so0n, alpha, beta);
+    soln_cell<CT, R, G, AB, true>(a, icl, so0n, alpha, beta);
 
     // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
 #pragma unroll
@@ -629,34 +712,44 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
             int const kind = a.gkind[jr];
             if (kind >= 0)
             {
-                R own[2 * NEQ + NEQ * ND];
-                load_rec<ND, R>(a.cur + row * D::RS, own);
+                R own[Rec<ND, R>::NUSED];
+                load_rec<ND, R>(a.cur + row * Rec<ND, R>::RS, own);
                 R g0[NEQ], g1[NEQ * ND], gt[NEQ];
                 bc0_ghost<ND, R>(kind, a.gnml + jr * ND, a.gval + jr * NEQ, so0n, g0);
                 bc1_ghost<ND, R>(kind, a.gnml + jr * ND, own + 2 * NEQ, g1);
-                solt_row<ND, R>(g0, g1, ldg(a.gamma + jr), gt);
-                store_rec<ND, R>(a.nxt + jr * D::RS, g0, gt, g1);
+                Prim<ND, R> const qg(g0, ldg(a.gamma + jr));
+                solt_prim<ND, R>(qg, g0, g1, gt);
+                store_rec<ND, R>(a.nxt + jr * Rec<ND, R>::RS, g0, gt, g1, qg);
             }
         }
     }
 
-    R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n);
+    R rinv;
+    R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n, rinv);
     R so1n[NEQ * ND];
     dsoln_cell<CT, R, G, AB>(a, icl, so0n, cflc, alpha, beta, so1n);
     R so0t[NEQ];
-    solt_row<ND, R>(so0n, so1n, ldg(a.gamma + row), so0t);
-    store_rec<ND, R>(a.nxt + row * D::RS, so0n, so0t, so1n);
+    Prim<ND, R> const q(so0n, ldg(a.gamma + row), rinv);
+    solt_prim<ND, R>(q, so0n, so1n, so0t);
+    store_rec<ND, R>(a.nxt + row * Rec<ND, R>::RS, so0n, so0t, so1n, q);
 }
 
 // The work of thread t of one substep: body cell t for t < ncell, ghost row
-// t - ncell after that.
-template <int ND, typename R, typename G>
+// t - ncell after that.  CT1 = 0 dispatches on each cell's type; a nonzero
+// CT1 compiles the one cell type of a single-type mesh, whose kernel then
+// needs only that type's registers.
+template <int ND, typename R, typename G, int CT1 = 0>
 __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t t)
 {
     if (t < a.ncell)
     {
         int const ct = a.ctype[t];
-        if constexpr (ND == 2)
+        if constexpr (CT1 != 0)
+        {
+            (void)ct;
+            fused_cell<CT1, R, G>(a, t);
+        }
+        else if constexpr (ND == 2)
         {
             if (ct == 4)
                 fused_cell<4, R, G>(a, t);
@@ -682,19 +775,20 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
         if (a.gkind[g] < 0)
         {
             constexpr int NEQ = ND + 2;
-            R rec[2 * NEQ + NEQ * ND];
-            load_rec<ND, R>(a.nxt + g * Dim<ND>::RS, rec);
+            R rec[Rec<ND, R>::NUSED];
+            load_rec<ND, R>(a.nxt + g * Rec<ND, R>::RS, rec);
             R tt[NEQ];
-            solt_row<ND, R>(rec, rec + 2 * NEQ, ldg(a.gamma + g), tt);
-            store_rec<ND, R>(a.nxt + g * Dim<ND>::RS, rec, tt, rec + 2 * NEQ);
+            Prim<ND, R> const q(rec, ldg(a.gamma + g));
+            solt_prim<ND, R>(q, rec, rec + 2 * NEQ, tt);
+            store_rec<ND, R>(a.nxt + g * Rec<ND, R>::RS, rec, tt, rec + 2 * NEQ, q);
         }
     }
 }
 
-template <int ND, typename R, typename G>
+template <int ND, typename R, typename G, int CT1 = 0>
 __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
 {
-    fused_thread<ND, R, G>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
 } // namespace dev
