@@ -195,6 +195,21 @@ int scg_euler_totals(scg_euler * core, double * out);
 int scg_euler_totals_noalloc(scg_euler * core, double * out);
 /* min and max of cflo over body cells (EulerField.calc_cfl_range). */
 int scg_euler_cfl_range(scg_euler * core, double * out);
+/* One scalar field of the newest solution (so0n) over the body cells, derived
+ * on the device in FP64 and copied to out[ncell]; replaces the properties of
+ * EulerField (solvcon/multidim/euler/_field.py:59-125), which derive the same
+ * fields on the host from a full copy of so0n.  which: SCG_FIELD_* below;
+ * SCG_FIELD_VELZ only in 3D, anything else SCG_EINVAL. */
+#define SCG_FIELD_DENSITY 0
+#define SCG_FIELD_VELX 1
+#define SCG_FIELD_VELY 2
+#define SCG_FIELD_VELZ 3
+#define SCG_FIELD_SPEED 4
+#define SCG_FIELD_PRESSURE 5
+#define SCG_FIELD_MACH 6
+#define SCG_FIELD_TOTAL_ENERGY 7
+#define SCG_FIELD_CFL 8
+int scg_euler_field(scg_euler * core, int which, double * out);
 /* Device memory held by the core, in bytes. */
 int scg_euler_device_bytes(const scg_euler * core, int64_t * out);
 

@@ -66,6 +66,7 @@ _SIGS = {
     "scg_euler_limiter_mask": ([_vp, _vp], ctypes.c_int),
     "scg_euler_totals": ([_vp, _vp], ctypes.c_int),
     "scg_euler_cfl_range": ([_vp, _vp], ctypes.c_int),
+    "scg_euler_field": ([_vp, ctypes.c_int, _vp], ctypes.c_int),
     "scg_euler_device_bytes": ([_vp, _vp], ctypes.c_int),
     "scg_euler_stream": ([_vp, _vp], ctypes.c_int),
     "scg_euler_profile": ([_vp, ctypes.c_int], ctypes.c_int),

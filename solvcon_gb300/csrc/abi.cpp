@@ -352,6 +352,11 @@ int scg_euler_cfl_range(scg_euler * core, double * out)
     return guarded([&] { need(core, "scg_euler_cfl_range")->c->cfl_range(out); });
 }
 
+int scg_euler_field(scg_euler * core, int which, double * out)
+{
+    return guarded([&] { need(core, "scg_euler_field")->c->field(which, out); });
+}
+
 int scg_euler_device_bytes(const scg_euler * core, int64_t * out)
 {
     return guarded([&] { *out = static_cast<int64_t>(need(core, "scg_euler_device_bytes")->c->device_bytes()); });

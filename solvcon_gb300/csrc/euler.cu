@@ -92,18 +92,18 @@ __global__ void k_soln(MarchArgs<R, G> a)
     if constexpr (ND == 2)
     {
         if (ct == 4)
-            soln_cell<4, R, G, false>(a, icl, so0n, nullptr, nullptr);
+            soln_cell<4, R, G>(a, icl, so0n);
         else
-            soln_cell<3, R, G, false>(a, icl, so0n, nullptr, nullptr);
+            soln_cell<3, R, G>(a, icl, so0n);
     }
     else
     {
         switch (ct)
         {
-        case 6: soln_cell<6, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
-        case 5: soln_cell<5, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
-        case 7: soln_cell<7, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
-        default: soln_cell<8, R, G, false>(a, icl, so0n, nullptr, nullptr); break;
+        case 6: soln_cell<6, R, G>(a, icl, so0n); break;
+        case 5: soln_cell<5, R, G>(a, icl, so0n); break;
+        case 7: soln_cell<7, R, G>(a, icl, so0n); break;
+        default: soln_cell<8, R, G>(a, icl, so0n); break;
         }
     }
     R * out = a.nxt + (icl + a.ngst) * Rec<ND, R>::RS;
@@ -156,18 +156,18 @@ __global__ void k_dsoln(MarchArgs<R, G> a)
     if constexpr (ND == 2)
     {
         if (ct == 4)
-            dsoln_cell<4, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g);
+            dsoln_cell<4, R, G>(a, icl, s, cflc, g);
         else
-            dsoln_cell<3, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g);
+            dsoln_cell<3, R, G>(a, icl, s, cflc, g);
     }
     else
     {
         switch (ct)
         {
-        case 6: dsoln_cell<6, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
-        case 5: dsoln_cell<5, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
-        case 7: dsoln_cell<7, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
-        default: dsoln_cell<8, R, G, false>(a, icl, s, cflc, nullptr, nullptr, g); break;
+        case 6: dsoln_cell<6, R, G>(a, icl, s, cflc, g); break;
+        case 5: dsoln_cell<5, R, G>(a, icl, s, cflc, g); break;
+        case 7: dsoln_cell<7, R, G>(a, icl, s, cflc, g); break;
+        default: dsoln_cell<8, R, G>(a, icl, s, cflc, g); break;
         }
     }
     for (int i = 0; i < NEQ * ND; ++i)
@@ -297,6 +297,52 @@ __global__ void k_from_f64(double const * in, R * out, int64_t n)
     {
         out[i] = R(in[i]);
     }
+}
+
+// One scalar field of the newest solution per body cell, in FP64, with the
+// formulas of EulerField (solvcon/multidim/euler/_field.py:80-125):
+// velocity m / rho, speed |v|, pressure (gamma - 1)(E - rho |v|^2 / 2), Mach
+// number |v| / sqrt(gamma p / rho), and the unclamped CFL number cflo.
+template <int ND, typename R>
+__global__ void k_field(R const * nxt, R const * gamma, R const * cflo, int64_t ngst, int64_t ncell, int which,
+                        double * out)
+{
+    int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (icl >= ncell)
+    {
+        return;
+    }
+    int64_t const row = icl + ngst;
+    R const * u = nxt + row * Rec<ND, R>::RS;
+    double const rho = double(u[0]);
+    double v[ND];
+    double vsq = 0.0;
+    for (int d = 0; d < ND; ++d)
+    {
+        v[d] = double(u[1 + d]) / rho;
+        vsq += v[d] * v[d];
+    }
+    double const energy = double(u[ND + 1]);
+    double const ga = double(gamma[row]);
+    double r = 0.0;
+    switch (which)
+    {
+    case EF_DENSITY: r = rho; break;
+    case EF_VELX: r = v[0]; break;
+    case EF_VELY: r = v[1]; break;
+    case EF_VELZ: r = v[ND - 1]; break;
+    case EF_SPEED: r = sqrt(vsq); break;
+    case EF_PRESSURE: r = (ga - 1.0) * (energy - 0.5 * rho * vsq); break;
+    case EF_MACH:
+    {
+        double const p = (ga - 1.0) * (energy - 0.5 * rho * vsq);
+        r = sqrt(vsq) / sqrt(ga * p / rho);
+        break;
+    }
+    case EF_TOTAL_ENERGY: r = energy; break;
+    default: r = double(cflo[row]); break;
+    }
+    out[icl] = r;
 }
 
 // Per-block FP64 partial sums of so0n[:, i] * clvol (Kahan inside a thread,
@@ -1214,6 +1260,27 @@ public:
         reduce(p, nb);
         out[0] = p[NEQ];
         out[1] = p[NEQ + 1];
+    }
+
+    void field(int which, double * out) override
+    {
+        if (which < 0 || which >= EF_COUNT || (which == EF_VELZ && ND != 3))
+        {
+            throw std::invalid_argument("EulerCore: unknown field " + std::to_string(which) + " in " +
+                                        std::to_string(ND) + "D");
+        }
+        if (ncell == 0)
+        {
+            return;
+        }
+        double * d = staging(ncell);
+        k_field<ND, R><<<grid_for(ncell), BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_gamma.ptr, d_cflo.ptr, ngstcell,
+                                                             ncell, which, d);
+        launched(stream, "field");
+        cuda_check(cudaMemcpyAsync(out, d, static_cast<size_t>(ncell) * sizeof(double), cudaMemcpyDeviceToHost,
+                                   stream),
+                   "D2H");
+        sync();
     }
 
 private:

@@ -57,6 +57,22 @@ enum EulerBCKind : int
     BC_INLET = 2,
 };
 
+// Scalar fields of the newest solution over the body cells, derived on the
+// device (the properties of EulerField, solvcon/multidim/euler/_field.py).
+enum EulerField : int
+{
+    EF_DENSITY = 0,
+    EF_VELX = 1,
+    EF_VELY = 2,
+    EF_VELZ = 3,
+    EF_SPEED = 4,
+    EF_PRESSURE = 5,
+    EF_MACH = 6,
+    EF_TOTAL_ENERGY = 7,
+    EF_CFL = 8,
+    EF_COUNT = 9,
+};
+
 // Precision of the march: state/flux arithmetic and stored geometry.
 enum Precision : int
 {
@@ -100,6 +116,8 @@ public:
     virtual void totals(double * out) = 0;
     // min and max of cflo over body cells.
     virtual void cfl_range(double * out) = 0;
+    // One EulerField scalar over the body cells, FP64, into host out[ncell].
+    virtual void field(int which, double * out) = 0;
 
     // Raw device view of the newest order-0 solution (so0n rows inside the
     // solution records), the cell volumes and the core's stream.

@@ -125,16 +125,12 @@ __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t
 
 // ---------------------------------------------------------------------------
 // calc_soln for one body cell (euler_march.cpp:197-303): the CESE flux
-// integral over the cell's BCEs, divided by the CCE volume.  For simplices it
-// also returns, per face and equation, the two halves of the gradient
-// element's solution deltas that need only neighbour data:
-//   alpha = so0c + hdt so0t + R . so1c,   beta = Q . so1c
-// so that calc_dsoln needs no second gather.
+// integral over the cell's BCEs, divided by the CCE volume.
 //
 // With CACHE set (the fused march, where every record's primitive cache is
 // valid) a neighbour's primitives come from its record.
-template <int CT, typename R, typename G, bool AB, bool CACHE = false>
-__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n, R * alpha, R * beta)
+template <int CT, typename R, typename G, bool CACHE = false>
+__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -209,30 +205,6 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
         {
             acc[i].add(-fl[i]);
         }
-        if constexpr (AB)
-        {
-            R rr[ND], qq[ND];
-#pragma unroll
-            for (int d = 0; d < ND; ++d)
-            {
-                rr[d] = fg<ND>(a, f, D::K_R + d, icl);
-                qq[d] = fg<ND>(a, f, D::K_Q + d, icl);
-            }
-#pragma unroll
-            for (int i = 0; i < NEQ; ++i)
-            {
-                R al = u[i] + a.hdt * t[i];
-                R be = R(0);
-#pragma unroll
-                for (int d = 0; d < ND; ++d)
-                {
-                    al += rr[d] * g[i * ND + d];
-                    be += qq[d] * g[i * ND + d];
-                }
-                alpha[f * NEQ + i] = al;
-                beta[f * NEQ + i] = be;
-            }
-        }
     }
     R const ivol = R(ldg(a.cgeo + 0 * a.ncell + icl));
 #pragma unroll
@@ -282,11 +254,13 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 
 // calc_dsoln for one body cell (euler_gradient.cpp:23-130 with the gradient
 // element of GradientElement.cpp:305-458): per fundamental gradient element
-// solve, W-1/2 weights, W-3/4 cap, weighted sum.  When AB is set the neighbour
-// terms come from soln_cell's alpha/beta; otherwise they are gathered here.
-template <int CT, typename R, typename G, bool AB>
+// solve, W-1/2 weights, W-3/4 cap, weighted sum.  The neighbour records are
+// gathered a second time (calc_soln just read them, so the loads hit in
+// cache); carrying calc_soln's neighbour terms over instead costs more FP64
+// operations and, in FP32, twice the registers and half the occupancy.
+template <int CT, typename R, typename G>
 __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
-                                           R const * alpha, R const * beta, R * so1n)
+                                           R * so1n)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -359,43 +333,28 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 
     // Solution deltas at the evaluation points: uf[f][i].
     R uf[NFC][NEQ];
-    if constexpr (AB)
+#pragma unroll
+    for (int f = 0; f < NFC; ++f)
     {
+        int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
+        R rec[Rec<ND, R>::NUSED];
+        load_rec<ND, R>(a.cur + jr * Rec<ND, R>::RS, rec);
+        R jd[ND];
 #pragma unroll
-        for (int f = 0; f < NFC; ++f)
+        for (int d = 0; d < ND; ++d)
         {
-#pragma unroll
-            for (int i = 0; i < NEQ; ++i)
-            {
-                uf[f][i] = alpha[f * NEQ + i] - so0n[i] + tau * beta[f * NEQ + i];
-            }
+            jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
         }
-    }
-    else
-    {
 #pragma unroll
-        for (int f = 0; f < NFC; ++f)
+        for (int i = 0; i < NEQ; ++i)
         {
-            int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
-            R rec[Rec<ND, R>::NUSED];
-            load_rec<ND, R>(a.cur + jr * Rec<ND, R>::RS, rec);
-            R jd[ND];
+            R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
 #pragma unroll
             for (int d = 0; d < ND; ++d)
             {
-                jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+                s += jd[d] * rec[2 * NEQ + i * ND + d];
             }
-#pragma unroll
-            for (int i = 0; i < NEQ; ++i)
-            {
-                R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
-#pragma unroll
-                for (int d = 0; d < ND; ++d)
-                {
-                    s += jd[d] * rec[2 * NEQ + i * ND + d];
-                }
-                uf[f][i] = s;
-            }
+            uf[f][i] = s;
         }
     }
 
@@ -690,17 +649,10 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
     constexpr int NFC = CellT<CT>::NFC;
-    // Simplices carry calc_dsoln's neighbour terms over from calc_soln's
-    // gather in FP32 (memory-bound: no second gather); in FP64 (FP64-pipe
-    // bound) calc_dsoln gathers again, which takes fewer FP64 operations
-    // and registers, and the second gather hits in cache.
-    constexpr bool AB = CellT<CT>::SIMPLEX && !Rec<ND, R>::PRIM;
     int64_t const row = icl + a.ngst;
 
     R so0n[NEQ];
-    R alpha[AB ? NFC * NEQ : 1];
-    R beta[AB ? NFC * NEQ : 1];
-    soln_cell<CT, R, G, AB, true>(a, icl, so0n, alpha, beta);
+    soln_cell<CT, R, G, true>(a, icl, so0n);
 
     // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
 #pragma unroll
@@ -727,7 +679,7 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     R rinv;
     R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n, rinv);
     R so1n[NEQ * ND];
-    dsoln_cell<CT, R, G, AB>(a, icl, so0n, cflc, alpha, beta, so1n);
+    dsoln_cell<CT, R, G>(a, icl, so0n, cflc, so1n);
     R so0t[NEQ];
     Prim<ND, R> const q(so0n, ldg(a.gamma + row), rinv);
     solt_prim<ND, R>(q, so0n, so1n, so0t);

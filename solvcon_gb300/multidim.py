@@ -289,9 +289,26 @@ class EulerCore:
 
     def cfl_range(self):
         """(min, max) of cflo over the body cells."""
+        self._flush()
         out = np.zeros(2, dtype="float64")
         check(lib.scg_euler_cfl_range(self._h, ptr(out)))
         return float(out[0]), float(out[1])
+
+    #: Scalar fields :meth:`device_field` derives on the device, by id.
+    DEVICE_FIELDS = {"density": 0, "velx": 1, "vely": 2, "velz": 3,
+                     "speed": 4, "pressure": 5, "mach": 6,
+                     "total_energy": 7, "cfl": 8}
+
+    def device_field(self, name):
+        """One scalar field of the newest solution over the body cells
+        (one of :attr:`DEVICE_FIELDS`), derived on the device in FP64; only
+        ``ncell`` doubles cross to the host."""
+        if name not in self.DEVICE_FIELDS:
+            raise ValueError("unknown field '%s'" % name)
+        self._flush()
+        out = np.zeros(max(self._ncell, 1), dtype="float64")
+        check(lib.scg_euler_field(self._h, self.DEVICE_FIELDS[name], ptr(out)))
+        return out[:self._ncell]
 
 
 def _make_prop(name):
