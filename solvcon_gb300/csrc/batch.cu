@@ -28,14 +28,31 @@ namespace
 
 using scg::dev::MarchArgs;
 
-template <int ND, typename R, typename G, int B>
+// CT1: the one cell type of every core (then only that type's path is
+// compiled and the kernel needs only its registers), or 0 for any mix.
+// Every thread of a tile works on the same core, so the tile's argument
+// block is staged once in shared memory and read from there as needed, as
+// the single-core kernel reads its parameters, instead of being held in
+// registers.
+template <int ND, typename R, typename G, int B, int CT1>
 __global__ void __launch_bounds__(B) k_fused_batch(MarchArgs<R, G> const * descs, int2 const * tiles, int ntiles)
 {
+    using Args = MarchArgs<R, G>;
+    static_assert(sizeof(Args) % sizeof(int) == 0, "argument block is whole words");
+    constexpr int NW = static_cast<int>(sizeof(Args) / sizeof(int));
+    static_assert(NW <= B, "one word per thread");
+    __shared__ __align__(16) int words[NW];
+    Args const & a = *reinterpret_cast<Args const *>(words);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
     {
         int2 const tl = tiles[t];
-        MarchArgs<R, G> const a = descs[tl.x];
-        scg::dev::fused_thread<ND, R, G>(a, static_cast<int64_t>(tl.y) + threadIdx.x);
+        __syncthreads(); // the previous tile is done with the block
+        if (threadIdx.x < NW)
+        {
+            words[threadIdx.x] = reinterpret_cast<int const *>(descs + tl.x)[threadIdx.x];
+        }
+        __syncthreads();
+        scg::dev::fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(tl.y) + threadIdx.x);
     }
 }
 
@@ -50,7 +67,7 @@ struct BatchBase
     double last_ms = 0.0; // device time of the last march's launches
 };
 
-template <int ND, typename R, typename G, int B>
+template <int ND, typename R, typename G, int B, int CT1>
 class Batch : public BatchBase
 {
 public:
@@ -96,7 +113,7 @@ public:
         int dev = 0, nsm = 0, occ = 0;
         scg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
         scg::cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
-        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fused_batch<ND, R, G, B>, B, 0),
+        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fused_batch<ND, R, G, B, CT1>, B, 0),
                         "occupancy");
         int64_t const resident = static_cast<int64_t>(nsm) * std::max(occ, 1);
         grid = persistent ? std::min<int64_t>(ntiles, resident) : ntiles;
@@ -147,8 +164,8 @@ public:
     {
         for (int p = 0; p < 2; ++p)
         {
-            k_fused_batch<ND, R, G, B><<<static_cast<unsigned>(grid), B, 0, stream>>>(descs[p].ptr, tiles.ptr,
-                                                                                 static_cast<int>(ntiles));
+            k_fused_batch<ND, R, G, B, CT1><<<static_cast<unsigned>(grid), B, 0, stream>>>(
+                descs[p].ptr, tiles.ptr, static_cast<int>(ntiles));
             scg::launched(stream, "fused_batch");
         }
     }
@@ -205,16 +222,34 @@ private:
     cudaEvent_t ev[2] = {nullptr, nullptr};
 };
 
-template <int ND, typename R, typename G>
-std::unique_ptr<BatchBase> make_for_block(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)
+template <int ND, typename R, typename G, int CT1>
+std::unique_ptr<BatchBase> make_for_type(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)
 {
     switch (block)
     {
-    case 64: return std::make_unique<Batch<ND, R, G, 64>>(std::move(cores), persistent);
-    case 128: return std::make_unique<Batch<ND, R, G, 128>>(std::move(cores), persistent);
-    case 256: return std::make_unique<Batch<ND, R, G, 256>>(std::move(cores), persistent);
+    case 64: return std::make_unique<Batch<ND, R, G, 64, CT1>>(std::move(cores), persistent);
+    case 128: return std::make_unique<Batch<ND, R, G, 128, CT1>>(std::move(cores), persistent);
+    case 256: return std::make_unique<Batch<ND, R, G, 256, CT1>>(std::move(cores), persistent);
     default: throw std::invalid_argument("EulerBatch: block must be 64, 128 or 256");
     }
+}
+
+// The simplex-only kernel when every core has only triangles (2D) or only
+// tetrahedra (3D), else the kernel that dispatches on each cell's type.
+template <int ND, typename R, typename G>
+std::unique_ptr<BatchBase> make_for_block(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)
+{
+    constexpr int SIMPLEX = (ND == 2) ? scg::CT_TRIANGLE : scg::CT_TET;
+    bool all = true;
+    for (auto * c : cores)
+    {
+        all = all && c->single_ct == SIMPLEX;
+    }
+    if (all)
+    {
+        return make_for_type<ND, R, G, SIMPLEX>(std::move(cores), block, persistent);
+    }
+    return make_for_type<ND, R, G, 0>(std::move(cores), block, persistent);
 }
 
 std::unique_ptr<BatchBase> make_batch(std::vector<scg::EulerCoreBase *> cores, int block, bool persistent)

@@ -1314,7 +1314,6 @@ private:
 
     int64_t nrow = 0;
     int nslot = 0;
-    int single_ct = -1; // the cell type if all cells share one, else -1
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     MeshView mv{};

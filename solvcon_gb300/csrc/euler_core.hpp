@@ -99,6 +99,7 @@ public:
     double time_increment = 0.0;
     double sigma0 = 3.0, taumin = 0.0, tauscale = 1.0;
     int precision = PREC_FP64;
+    int single_ct = -1; // the cell type if every body cell has it, else -1
 
     // Array shape in the reference layout; nghost is the first-axis ghost count.
     void array_shape(int which, int64_t * shape, int * nd, int64_t * nghost) const;
