@@ -245,11 +245,43 @@ def time_e2e(core, steps):
     return (t1 - t0) * 1e3, h2d, d2h
 
 
-def _oracle_worker(workload, nside, seed_offset, warmup, steps, barrier, out):
-    """One CPU process of the oracle throughput run: build its own sample,
-    warm up, wait for the others, march, report (cells, seconds)."""
+def tube_state(ncoord, seed):
+    """The 1D workload: a Sod-type tube on [-1, 1] (random left/right
+    density and pressure, at rest), its dt for CFL 0.8."""
+    from solvcon_gb300.serving import sod_tube_state
+    return sod_tube_state(ncoord, seed)
+
+
+def scalar_state(ncelm):
+    """The spacetime workload: sin(x) / cos(x) on [0, 2 pi] with ncelm
+    conservation elements, dt for CFL 0.8 at unit wave speed; returns the
+    grid, so0, so1 (whole tables) and dt."""
+    from solvcon_gb300.spacetime import Grid
+    grid = Grid(0.0, 2.0 * np.pi, int(ncelm))
+    x = np.asarray(grid.xcoord)
+    dt = 0.8 * (2.0 * np.pi / ncelm)
+    return grid, np.sin(x), np.cos(x), dt
+
+
+def _oracle_setup(workload, size, seed_offset):
+    """One seeded sample of a workload on the CPU oracle: returns (units per
+    step, march(steps))."""
     from oracle import oracle as ora
-    w, mesh, state, faces = make_workload(workload, nside=nside,
+    if workload == "tube1d":
+        x, so0, dt = tube_state(size, 2026 + seed_offset)
+        o = ora.OracleEuler1D(size, dt)
+        o.coord[:] = x
+        o.so0[:] = so0
+        o.setup_march()
+        return size, lambda k: o.march_alpha(2, k)
+    if workload == "spacetime":
+        grid, so0, so1, dt = scalar_state(size)
+        o = ora.OracleSpacetime(0, grid.xcoord, dt)
+        o.so0[:] = so0
+        o.so1[:] = so1
+        o.setup_march()
+        return grid.xsize - 4, lambda k: o.march_alpha(2, k)
+    w, mesh, state, faces = make_workload(workload, nside=size,
                                           seed_offset=seed_offset)
     o = ora.OracleEuler(mesh, 1e-4)
     o.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
@@ -257,18 +289,25 @@ def _oracle_worker(workload, nside, seed_offset, warmup, steps, barrier, out):
     o.add_slipwall(faces)
     o.call("bc_soln")
     o.call("bc_dsoln")
-    o.march(warmup)
+    return mesh.ncell, o.march
+
+
+def _oracle_worker(workload, size, seed_offset, warmup, steps, barrier, out):
+    """One CPU process of the oracle throughput run: build its own sample,
+    warm up, wait for the others, march, report (units, seconds)."""
+    units, march = _oracle_setup(workload, size, seed_offset)
+    march(warmup)
     barrier.wait()
     t0 = time.perf_counter()
-    o.march(steps)
-    out.put((mesh.ncell, time.perf_counter() - t0))
+    march(steps)
+    out.put((units, time.perf_counter() - t0))
 
 
-def oracle_throughput(workload, nside, steps, warmup=1, nproc=None):
+def oracle_throughput(workload, size, steps, warmup=1, nproc=None):
     """The CPU oracle (restatement of the reference march, which is serial)
     on every host core at once: one process per core, each marching its own
-    seeded sample of the workload.  Returns (aggregate cell-steps/s over the
-    wall time of the concurrent marches, cells per sample, processes,
+    seeded sample of the workload.  Returns (aggregate unit-steps/s over the
+    wall time of the concurrent marches, units per sample, processes,
     seconds).  Processes are spawned, never forked (the parent may already
     hold a CUDA context)."""
     import multiprocessing as mp
@@ -277,7 +316,7 @@ def oracle_throughput(workload, nside, steps, warmup=1, nproc=None):
     barrier = ctx.Barrier(nproc + 1)
     out = ctx.Queue()
     procs = [ctx.Process(target=_oracle_worker,
-                         args=(workload, nside, 7919 * (k + 1), warmup, steps,
+                         args=(workload, size, 7919 * (k + 1), warmup, steps,
                                barrier, out)) for k in range(nproc)]
     for p in procs:
         p.start()
@@ -287,12 +326,16 @@ def oracle_throughput(workload, nside, steps, warmup=1, nproc=None):
     t1 = time.perf_counter()
     for p in procs:
         p.join()
-    cells = res[0][0]
-    return sum(c for c, _ in res) * steps / (t1 - t0), cells, nproc, t1 - t0
+    units = res[0][0]
+    return sum(c for c, _ in res) * steps / (t1 - t0), units, nproc, t1 - t0
 
 
 def cpu_nside(workload, steps):
     """Sample resolution giving about 30 s of oracle work per process."""
+    if workload == "tube1d":
+        return int(min(1000001, 16e6 * 30.0 / max(steps, 1))) | 1
+    if workload == "spacetime":
+        return int(min(4000000, 40e6 * 30.0 / max(steps, 1)))
     w = WORKLOADS[workload]
     if w["ndim"] == 2:
         cells = 0.35e6 * 30.0 / max(steps, 1)
@@ -326,32 +369,188 @@ def barrier(dist):
         dist.barrier()
 
 
+LINE_WORKLOADS = {
+    "tube1d": ("point-steps/s", 20000001,
+               "1D Euler CESE march (Euler1DCore.march_alpha2) of a Sod-type "
+               "tube on [-1, 1], %d points, gamma 1.4, CFL 0.8, FP64"),
+    "spacetime": ("point-steps/s", 20000000,
+                  "spacetime linear-scalar CESE march (march_alpha2) of "
+                  "sin(x) on [0, 2 pi], %d conservation elements (a point "
+                  "is a solution element of either plane), CFL 0.8, FP64"),
+}
+
+# Algorithmic HBM bytes per point-step of the 1D marches (FP64): Euler1DCore
+# reads so0, so1, coord, gamma and writes so0, so1, cfl (120 B); the linear
+# scalar reads so0, so1, x and writes so0, so1, cfl (48 B).
+LINE_ALG_BYTES = {"tube1d": 120, "spacetime": 48}
+
+
 def run_reference(args, world, rank, dist):
     if rank != 0:
         return
-    w = WORKLOADS[args.workload]
-    nside = args.cpu_nside or cpu_nside(args.workload, args.steps + args.warmup)
-    value, cells, nproc, secs = oracle_throughput(args.workload, nside,
+    size = args.cpu_nside or cpu_nside(args.workload, args.steps + args.warmup)
+    value, units, nproc, secs = oracle_throughput(args.workload, size,
                                                   args.steps, args.warmup)
+    if args.workload in LINE_WORKLOADS:
+        unit, _, desc = LINE_WORKLOADS[args.workload]
+        desc = desc % (args.nside or LINE_WORKLOADS[args.workload][1])
+        what = "%d-point" % units
+    else:
+        unit = "cell-steps/s"
+        desc = _desc(WORKLOADS[args.workload])
+        what = "%d-cell" % units
     sample = ("%d processes (one per host core), each marching its own "
-              "%d-cell seeded sample of the %s workload (same generator, "
-              "nside=%d) for %d steps after %d warm-up steps; the reference "
-              "march is serial, so a core runs one mesh"
-              % (nproc, cells, args.workload, nside, args.steps, args.warmup))
+              "%s seeded sample of the %s workload (same generator, "
+              "size %d) for %d steps after %d warm-up steps; the reference "
+              "march is serial, so a core runs one sample"
+              % (nproc, what, args.workload, size, args.steps, args.warmup))
     line = {
-        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
+        "metric": unit, "value": value, "unit": unit,
         "impl": "reference", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "%s (%s)" % (args.workload, _desc(w)),
-                   "sample_cells": cells, "precision": "fp64"},
-        "cpu_baseline": {"value": value, "unit": "cell-steps/s",
+        "config": {"workload": "%s (%s)" % (args.workload, desc),
+                   "sample_units": units, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": unit,
                          "cores": nproc, "kind": "port", "sample": sample},
-        "e2e": {"value": value, "unit": "cell-steps/s",
+        "e2e": {"value": value, "unit": unit,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_line(args, world, rank, dist):
+    """The 1D marches (Euler1DCore, spacetime linear scalar): point-steps/s
+    with the state resident (CUDA events on the solver's stream around K
+    steps replayed from the solver's CUDA graph), e2e through the C ABI with
+    so0/so1 copied from and back to pinned host memory every step, the
+    roofline on the algorithmic bytes, and the oracle on every host core."""
+    from solvcon_gb300._lib import check, launch_count, lib
+    unit, default, desc = LINE_WORKLOADS[args.workload]
+    n = args.nside or default
+    if args.workload == "tube1d":
+        from solvcon_gb300 import onedim
+        n |= 1
+        x, so0, dt = tube_state(n, 2026 + rank)
+        core = onedim.Euler1DCore(n, dt)
+        core.coord[...] = x
+        core.so0[...] = so0
+        core.so1.fill(0.0)
+        core.gamma.fill(1.4)
+        core.cfl.fill(0.0)
+        core.setup_march()
+        core.release_views()
+        h, l1 = core._h, onedim.lib
+        march = lambda k: check(l1.scg_e1d_march(h, 2, k))  # noqa: E731
+        sync = lambda: check(l1.scg_e1d_sync(h))  # noqa: E731
+        stream = ctypes.c_void_p()
+        check(l1.scg_e1d_stream(h, ctypes.byref(stream)))
+        points = n
+        io = [(0, onedim._IDS["so0"], 3 * n), (0, onedim._IDS["so1"], 3 * n)]
+        get = lambda i, b, c: check(l1.scg_e1d_get(h, i, b, c))  # noqa: E731
+        put = lambda i, b, c: check(l1.scg_e1d_set(h, i, b, c))  # noqa: E731
+    else:
+        from solvcon_gb300 import spacetime as st
+        grid, so0, so1, dt = scalar_state(n)
+        svr = st.LinearScalarSolver(grid, dt)
+        sz = grid.xsize
+        for name, val in (("so0", so0), ("so1", so1)):
+            buf = np.ascontiguousarray(val, dtype="float64")
+            check(st.lib.scg_st_set(svr._h, svr._IDS[name],
+                                    buf.ctypes.data, sz))
+        svr.setup_march()
+        h, l1 = svr._h, st.lib
+        march = lambda k: check(l1.scg_st_march(h, 2, k))  # noqa: E731
+        sync = lambda: check(l1.scg_st_sync(h))  # noqa: E731
+        stream = ctypes.c_void_p()
+        check(l1.scg_st_stream(h, ctypes.byref(stream)))
+        points = grid.xsize - 4  # both planes: 2 ncelm + 1 solution points
+        io = [(0, svr._IDS["so0"], sz), (0, svr._IDS["so1"], sz)]
+        get = lambda i, b, c: check(l1.scg_st_get(h, i, b, c))  # noqa: E731
+        put = lambda i, b, c: check(l1.scg_st_set(h, i, b, c))  # noqa: E731
+    march(args.warmup)
+    sync()
+    e0, e1 = ctypes.c_void_p(), ctypes.c_void_p()
+    check(lib.scg_event_create(ctypes.byref(e0)))
+    check(lib.scg_event_create(ctypes.byref(e1)))
+    barrier(dist)
+    n0 = launch_count()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        check(lib.scg_event_record(e0, stream))
+        march(args.steps)
+        check(lib.scg_event_record(e1, stream))
+        sync()
+    launches = launch_count() - n0
+    ms = ctypes.c_double()
+    check(lib.scg_event_elapsed(e0, e1, ctypes.byref(ms)))
+    check(lib.scg_event_destroy(e0))
+    check(lib.scg_event_destroy(e1))
+    barrier(dist)
+    ms_max = reduce_max(dist, ms.value)
+    value = world * points * args.steps / (ms_max * 1e-3)
+
+    # e2e: host state in, one step, host state out, every step.
+    e2e_steps = args.e2e_steps or 5
+    bufs = []
+    for _, i, c in io:
+        p = ctypes.c_void_p()
+        check(lib.scg_host_alloc(c * 8, ctypes.byref(p)))
+        bufs.append((i, p, c))
+        get(i, p, c)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for i, p, c in bufs:
+            put(i, p, c)
+        march(1)
+        for i, p, c in bufs:
+            get(i, p, c)
+    e2e_s = time.perf_counter() - t0
+    nbytes = sum(c * 8 for _, _, c in bufs)
+    for _, p, _ in bufs:
+        check(lib.scg_host_free(p))
+    e2e_value = world * points * e2e_steps / reduce_max(dist, e2e_s)
+
+    hbm_peak, peak_kind = peaks()
+    achieved = LINE_ALG_BYTES[args.workload] * points * args.steps / \
+        (ms.value * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        size = args.cpu_nside or cpu_nside(args.workload, args.cpu_steps)
+        rate, units, nproc, secs = oracle_throughput(args.workload, size,
+                                                     args.cpu_steps)
+        cpu = {"value": rate, "unit": unit, "cores": nproc, "kind": "port",
+               "sample": "%d processes (one per host core), each marching "
+                         "its own %d-point sample for %d steps; %.1f s"
+                         % (nproc, units, args.cpu_steps, secs)}
+    line = {
+        "metric": unit, "value": value, "unit": unit, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "%s (%s)" % (args.workload, desc % n),
+                   "points": points, "dt": dt,
+                   "l2": "state larger than L2 (no flush needed)"
+                   if points * LINE_ALG_BYTES[args.workload] > 2e8 else
+                   "state fits in L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": None,
+                     "alg_bytes_per_point_step":
+                         LINE_ALG_BYTES[args.workload],
+                     "kernel": "one march step (two fused half-step kernels)",
+                     "step_ms": ms.value / args.steps,
+                     "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": unit,
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "steps": e2e_steps},
+        "gpu_launches": launches, "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def batch_meshes(nmesh, seed=2026, lo=2000, hi=200000):
@@ -724,7 +923,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tri2d",
                     choices=sorted(WORKLOADS) + ["batch", "serve",
-                                                 "accuracy"])
+                                                 "accuracy"] +
+                    sorted(LINE_WORKLOADS))
     ap.add_argument("--precision", default=None,
                     choices=["fp64", "fp32", "fp32-geom64"])
     ap.add_argument("--nside", type=int, default=None)
@@ -744,11 +944,13 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         return
-    if args.workload in ("batch", "serve", "accuracy"):
+    if args.workload in ("batch", "serve", "accuracy") or (
+            args.workload in LINE_WORKLOADS and args.impl != "reference"):
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
         import solvcon_gb300  # noqa: F401
-        {"batch": run_batch, "serve": run_serve,
-         "accuracy": run_accuracy}[args.workload](args, world, rank, dist)
+        {"batch": run_batch, "serve": run_serve, "accuracy": run_accuracy,
+         "tube1d": run_line, "spacetime": run_line}[args.workload](
+             args, world, rank, dist)
         if dist is not None:
             dist.destroy_process_group()
         return

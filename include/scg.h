@@ -317,6 +317,9 @@ int scg_st_op(scg_st * solver, int op, int odd_plane, int alpha);
 /* march_alpha<alpha>(steps): core.hpp:1027-1036.  Asynchronous. */
 int scg_st_march(scg_st * solver, int alpha, int64_t steps);
 int scg_st_sync(scg_st * solver);
+/* The solver's CUDA stream (cudaStream_t), for stream-ordered event timing
+ * (no reference counterpart: measurement plumbing). */
+int scg_st_stream(const scg_st * solver, void ** out);
 
 /* ------------------------------------------------------------------------
  * Timing and host-memory helpers (no reference counterpart: measurement

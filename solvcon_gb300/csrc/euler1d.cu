@@ -50,6 +50,7 @@ struct E1DArgs
 struct K1D
 {
     double x, xneg, xpos;
+    double r; // 1 / (rho + tiny), shared with update_cfl at the same point
     double up[3];
     double ll[3]; // flux through the lower-left of the CE to the right
     double lr[3]; // flux through the lower-right of the CE to the left
@@ -69,6 +70,7 @@ __device__ __forceinline__ void derive(E1DArgs const & a, int64_t ic, K1D & k)
         ux[i] = a.so1[ic * 3 + i];
     }
     double const r = 1.0 / (u[0] + TINY1D);
+    k.r = r;
     double const r2 = r * r;
     double const m2r2 = u[1] * u[1] * r2; // u1^2 / u0^2
     double jac[3][3];
@@ -110,17 +112,24 @@ __device__ __forceinline__ void derive(E1DArgs const & a, int64_t ic, K1D & k)
     }
 }
 
-// update_cfl at one point (Euler1DCore.cpp:70-94).
-__device__ __forceinline__ void cfl_at(E1DArgs const & a, int64_t it, double hdt)
+// update_cfl at one point (Euler1DCore.cpp:70-94).  The reference's three
+// divisions by rho use r = 1 / (rho + tiny), the reciprocal the kernel
+// derivation at the same point forms (equal unless rho < ~1e-84, where the
+// reference itself overflows).
+__device__ __forceinline__ double rho_recip(E1DArgs const & a, int64_t it)
+{
+    return 1.0 / (a.so0[it * 3 + 0] + TINY1D);
+}
+
+__device__ __forceinline__ void cfl_at(E1DArgs const & a, int64_t it, double hdt, double r)
 {
     double const ga = a.gamma[it];
-    double const rho = a.so0[it * 3 + 0];
     double m2 = a.so0[it * 3 + 1];
     m2 *= m2;
-    double const ke = m2 / (2.0 * rho);
+    double const ke = 0.5 * m2 * r;
     double pr = (ga - 1.0) * (a.so0[it * 3 + 2] - ke);
     pr = (pr + fabs(pr)) / 2.0;
-    double const wspd = sqrt(ga * pr / rho) + sqrt(m2) / rho;
+    double const wspd = sqrt(ga * pr * r) + sqrt(m2) * r;
     double const dxpos = a.coord[it + 1] - a.coord[it];
     double const dxneg = a.coord[it] - a.coord[it - 1];
     a.cfl[it] = hdt * wspd / (dxpos < dxneg ? dxpos : dxneg);
@@ -149,7 +158,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
 {
     __shared__ double s_lr[B1D + 1][3];
     __shared__ double s_up[B1D + 1][3];
-    __shared__ double s_dxr[B1D + 1];
+    __shared__ double s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
     int64_t const j0 = static_cast<int64_t>(blockIdx.x) * B1D;
     int64_t const j = j0 + threadIdx.x;
     K1D k;
@@ -162,7 +171,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
             s_lr[threadIdx.x][i] = k.lr[i];
             s_up[threadIdx.x][i] = k.up[i];
         }
-        s_dxr[threadIdx.x] = k.x - k.xneg;
+        s_idxr[threadIdx.x] = 1.0 / (k.x - k.xneg);
     }
     if (threadIdx.x == 0)
     {
@@ -176,7 +185,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
                 s_lr[B1D][i] = h.lr[i];
                 s_up[B1D][i] = h.up[i];
             }
-            s_dxr[B1D] = h.x - h.xneg;
+            s_idxr[B1D] = 1.0 / (h.x - h.xneg);
         }
     }
     __syncthreads();
@@ -186,10 +195,10 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
         double v[3];
         if (DO_SO0)
         {
-            double const dx = a.coord[ic + 2] - a.coord[ic];
+            double const idx = 1.0 / (a.coord[ic + 2] - a.coord[ic]);
             for (int i = 0; i < 3; ++i)
             {
-                v[i] = (k.ll[i] + s_lr[threadIdx.x + 1][i]) / dx;
+                v[i] = (k.ll[i] + s_lr[threadIdx.x + 1][i]) * idx;
                 a.so0[(ic + 1) * 3 + i] = v[i];
             }
         }
@@ -202,16 +211,16 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
         }
         if (DO_CFL)
         {
-            cfl_at(a, ic, a.hdt);
+            cfl_at(a, ic, a.hdt, k.r);
         }
         if constexpr (ALPHA > 0)
         {
-            double const dn = k.xpos - k.x;
-            double const dp = s_dxr[threadIdx.x + 1];
+            double const idn = 1.0 / (k.xpos - k.x);
+            double const idp = s_idxr[threadIdx.x + 1];
             for (int i = 0; i < 3; ++i)
             {
-                double const duxn = (v[i] - k.up[i]) / dn;
-                double const duxp = (s_up[threadIdx.x + 1][i] - v[i]) / dp;
+                double const duxn = (v[i] - k.up[i]) * idn;
+                double const duxp = (s_up[threadIdx.x + 1][i] - v[i]) * idp;
                 a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
             }
         }
@@ -235,7 +244,8 @@ __global__ void k_cfl1d(E1DArgs a, int64_t start, int64_t nout)
     int64_t const j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j < nout)
     {
-        cfl_at(a, start + 2 * j, a.hdt);
+        int64_t const it = start + 2 * j;
+        cfl_at(a, it, a.hdt, rho_recip(a, it));
     }
 }
 

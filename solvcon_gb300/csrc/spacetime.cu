@@ -30,42 +30,79 @@ namespace
 struct STArgs
 {
     double const * x;
+    double const * geo; // [G_COUNT][xsize] grid quantities per point
     double * so0;
     double * so1;
     double * cfl;
-    int64_t ncelm;
+    int64_t ncelm, xsize;
     double hdt, qdt;
 };
 
-template <int KIND>
-struct Selm
+// Grid quantities of solution point xi, stored once (k_st_geo) with the very
+// expressions the reference evaluates on every half step
+// (SolutionElement::xctr/dxneg/dxpos/xn/xp, core.hpp:300-360; the CFL
+// half-width and the conservation-element width of
+// update_cfl/march_half_so0, core.hpp:962-980), so the march reads them
+// instead of recomputing them and its results stay bit-identical.
+enum
 {
-    double x, xneg, xpos, u, ux;
+    G_DXNEG = 0, // x - xneg
+    G_DXPOS,     // xpos - x
+    G_DMNEG,     // 0.5 (x + xneg) - xctr
+    G_DMPOS,     // 0.5 (x + xpos) - xctr
+    G_DISP,      // x - xctr
+    G_HDX,       // min(x - xneg, xpos - x)
+    G_WIDTH,     // xpos - xneg (the width of the element whose top is xi)
+    G_COUNT
+};
 
-    __device__ Selm(STArgs const & a, int64_t xi)
-        : x(a.x[xi])
-        , xneg(a.x[xi - 1])
-        , xpos(a.x[xi + 1])
-        , u(a.so0[xi])
-        , ux(a.so1[xi])
+__global__ void k_st_geo(double const * x, int64_t xsize, double * geo)
+{
+    int64_t const xi = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (xi < 1 || xi >= xsize - 1)
     {
+        return;
     }
-    __device__ double xctr() const { return (xneg + xpos) / 2; }
-    __device__ double dxneg() const { return x - xneg; }
-    __device__ double dxpos() const { return xpos - x; }
-    __device__ double xn() const { return dxneg() * (u + (0.5 * (x + xneg) - xctr()) * ux); }
-    __device__ double xp() const { return dxpos() * (u + (0.5 * (x + xpos) - xctr()) * ux); }
-    // Temporal flux of the forward branch (LinearScalarSelm::tp,
-    // InviscidBurgersSelm::tp).
-    __device__ double tp(STArgs const & a) const
+    double const xm = x[xi - 1], x0 = x[xi], xp = x[xi + 1];
+    double const xctr = (xm + xp) / 2;
+    double const dn = x0 - xm;
+    double const dp = xp - x0;
+    geo[G_DXNEG * xsize + xi] = dn;
+    geo[G_DXPOS * xsize + xi] = dp;
+    geo[G_DMNEG * xsize + xi] = 0.5 * (x0 + xm) - xctr;
+    geo[G_DMPOS * xsize + xi] = 0.5 * (x0 + xp) - xctr;
+    geo[G_DISP * xsize + xi] = x0 - xctr;
+    geo[G_HDX * xsize + xi] = dn < dp ? dn : dp;
+    geo[G_WIDTH * xsize + xi] = xp - xm;
+}
+
+__device__ __forceinline__ double gq(STArgs const & a, int k, int64_t xi) { return a.geo[k * a.xsize + xi]; }
+
+// The parts of solution element xi that the conservation elements on either
+// side of it use (LinearScalarSelm / InviscidBurgersSelm, xn, xp, tp, so0p):
+// ll = xp + tp (to the element on its right), ur = xn - tp (to the element on
+// its left), the value so0p at the next time level and dxneg, dxpos.
+template <int KIND>
+struct SelmParts
+{
+    double ll, ur, so0p, dxneg, dxpos;
+
+    __device__ SelmParts(STArgs const & a, int64_t xi)
     {
-        double const disp = x - xctr();
+        double const u = a.so0[xi];
+        double const ux = a.so1[xi];
+        dxneg = gq(a, G_DXNEG, xi);
+        dxpos = gq(a, G_DXPOS, xi);
+        double const disp = gq(a, G_DISP, xi);
+        double const xn = dxneg * (u + gq(a, G_DMNEG, xi) * ux);
+        double const xp = dxpos * (u + gq(a, G_DMPOS, xi) * ux);
+        double tp;
         if constexpr (KIND == 0)
         {
             double r = u;
             r += disp * ux;
             r -= a.qdt * ux;
-            return a.hdt * r;
+            tp = a.hdt * r;
         }
         else
         {
@@ -73,24 +110,21 @@ struct Selm
             double r = 0.5 * u2;
             r += disp * u * ux;
             r -= a.qdt * u2 * ux;
-            return a.hdt * r;
+            tp = a.hdt * r;
         }
-    }
-    __device__ double so0p(STArgs const & a) const
-    {
-        double r = u;
-        r += (x - xctr()) * ux;
-        r -= a.hdt * ux;
-        return r;
+        ll = xp + tp;
+        ur = xn - tp;
+        double q = u;
+        q += disp * ux;
+        q -= a.hdt * ux;
+        so0p = q;
     }
 };
 
 template <int KIND>
 __device__ __forceinline__ void cfl_at(STArgs const & a, int64_t xi)
 {
-    double const dn = a.x[xi] - a.x[xi - 1];
-    double const dp = a.x[xi + 1] - a.x[xi];
-    double const hdx = dn < dp ? dn : dp;
+    double const hdx = gq(a, G_HDX, xi);
     if constexpr (KIND == 0)
         a.cfl[xi] = a.hdt / hdx;
     else
@@ -109,27 +143,58 @@ __device__ __forceinline__ double wgrad(double duxn, double duxp)
     return (fap * duxn + fan * duxp) / (fap + fan + DBL_MIN);
 }
 
+constexpr int BST = 256;
+
 // One half step; STAGE bits: 1 so0, 2 cfl of the top element, 4 so1,
-// 8 periodic ghost copies (first half only).
+// 8 periodic ghost copies (first half only).  Thread t of a block derives
+// the parts of the lower-left solution element of conservation element
+// ic = block * BST + t - odd; the element's lower-right solution element is
+// the next thread's (or, for the last thread, one extra derived by thread 0),
+// shared through shared memory, so each solution element is derived once.
 template <int KIND, int ALPHA, int STAGE>
-__global__ void k_st_half(STArgs a, int odd)
+__global__ void __launch_bounds__(BST) k_st_half(STArgs a, int odd)
 {
-    int64_t const ic = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x - (odd ? 1 : 0);
+    __shared__ double s_ur[BST + 1];
+    __shared__ double s_so0p[BST + 1];
+    __shared__ double s_dxneg[BST + 1];
+    int64_t const ic0 = static_cast<int64_t>(blockIdx.x) * BST - (odd ? 1 : 0);
+    int64_t const ic = ic0 + threadIdx.x;
+    // Solution elements exist for ic <= ncelm (the last one is the
+    // lower-right element of conservation element ncelm - 1).
+    bool const selm = ic <= a.ncelm;
+    double ll = 0.0, so0pn = 0.0, dxposn = 1.0;
+    if (selm)
+    {
+        SelmParts<KIND> const sn(a, 2 + 2 * ic + odd);
+        ll = sn.ll;
+        so0pn = sn.so0p;
+        dxposn = sn.dxpos;
+        s_ur[threadIdx.x] = sn.ur;
+        s_so0p[threadIdx.x] = sn.so0p;
+        s_dxneg[threadIdx.x] = sn.dxneg;
+    }
+    if (threadIdx.x == 0)
+    {
+        int64_t const ich = ic0 + BST;
+        if (ich <= a.ncelm)
+        {
+            SelmParts<KIND> const sh(a, 2 + 2 * ich + odd);
+            s_ur[BST] = sh.ur;
+            s_so0p[BST] = sh.so0p;
+            s_dxneg[BST] = sh.dxneg;
+        }
+    }
+    __syncthreads();
     if (ic >= a.ncelm)
     {
         return;
     }
-    int64_t const xn_i = 2 + 2 * ic + odd;
-    int64_t const xt = xn_i + 1;
+    int64_t const xt = 3 + 2 * ic + odd;
     int64_t const last = 2 * a.ncelm + 1; // selm(ncelm - 1, odd plane)
-    Selm<KIND> const sn(a, xn_i);
-    Selm<KIND> const sp(a, xn_i + 2);
     double utp;
     if (STAGE & 1)
     {
-        double const ll = sn.xp() + sn.tp(a);
-        double const ur = sp.xn() - sp.tp(a);
-        utp = (ll + ur) / (a.x[xt + 1] - a.x[xt - 1]);
+        utp = (ll + s_ur[threadIdx.x + 1]) / gq(a, G_WIDTH, xt);
         a.so0[xt] = utp;
         if (STAGE & 8)
         {
@@ -156,8 +221,8 @@ __global__ void k_st_half(STArgs a, int odd)
     }
     if (STAGE & 4)
     {
-        double const duxn = (utp - sn.so0p(a)) / sn.dxpos();
-        double const duxp = (sp.so0p(a) - utp) / sp.dxneg();
+        double const duxn = (utp - so0pn) / dxposn;
+        double const duxp = (s_so0p[threadIdx.x + 1] - utp) / s_dxneg[threadIdx.x + 1];
         double const g = wgrad<ALPHA>(duxn, duxp);
         a.so1[xt] = g;
         if (STAGE & 8)
@@ -210,10 +275,12 @@ public:
         xsize = 2 * ncelm + 5;
         scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         x.alloc(static_cast<size_t>(xsize));
+        geo.alloc(static_cast<size_t>(G_COUNT * xsize));
         so0.alloc(static_cast<size_t>(xsize));
         so1.alloc(static_cast<size_t>(xsize));
         cfl.alloc(static_cast<size_t>(xsize));
         put(x.ptr, xcoord);
+        make_geo();
         std::vector<double> z(static_cast<size_t>(xsize), 0.0);
         put(so0.ptr, z.data());
         put(so1.ptr, z.data());
@@ -242,7 +309,20 @@ public:
         }
     }
 
-    STArgs args() { return STArgs{x.ptr, so0.ptr, so1.ptr, cfl.ptr, ncelm, 0.5 * time_increment, 0.25 * time_increment}; }
+    STArgs args()
+    {
+        return STArgs{x.ptr, geo.ptr, so0.ptr, so1.ptr, cfl.ptr, ncelm, xsize, 0.5 * time_increment,
+                      0.25 * time_increment};
+    }
+
+    // The grid quantities, after the coordinates are set.
+    void make_geo()
+    {
+        scg::cuda_check(cudaMemsetAsync(geo.ptr, 0, geo.bytes(), stream), "memset");
+        k_st_geo<<<static_cast<unsigned>((xsize + 255) / 256), 256, 0, stream>>>(x.ptr, xsize, geo.ptr);
+        scg::launched(stream, "spacetime_geo");
+        sync();
+    }
 
     double * field(int which)
     {
@@ -260,20 +340,20 @@ public:
     void half_t(int alpha, int odd)
     {
         int64_t const n = ncelm + (odd ? 1 : 0);
-        unsigned const grid = static_cast<unsigned>((n + 255) / 256);
+        unsigned const grid = static_cast<unsigned>((n + BST - 1) / BST);
         if (kind == 0)
         {
             if (alpha == 1)
-                k_st_half<0, 1, STAGE><<<grid, 256, 0, stream>>>(args(), odd);
+                k_st_half<0, 1, STAGE><<<grid, BST, 0, stream>>>(args(), odd);
             else
-                k_st_half<0, 2, STAGE><<<grid, 256, 0, stream>>>(args(), odd);
+                k_st_half<0, 2, STAGE><<<grid, BST, 0, stream>>>(args(), odd);
         }
         else
         {
             if (alpha == 1)
-                k_st_half<1, 1, STAGE><<<grid, 256, 0, stream>>>(args(), odd);
+                k_st_half<1, 1, STAGE><<<grid, BST, 0, stream>>>(args(), odd);
             else
-                k_st_half<1, 2, STAGE><<<grid, 256, 0, stream>>>(args(), odd);
+                k_st_half<1, 2, STAGE><<<grid, BST, 0, stream>>>(args(), odd);
         }
         scg::launched(stream, "spacetime_half");
     }
@@ -375,6 +455,10 @@ public:
     void set(int which, double const * host)
     {
         put(field(which), host);
+        if (which == 0)
+        {
+            make_geo();
+        }
     }
 
     void sync() { scg::cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
@@ -395,7 +479,7 @@ private:
         sync();
     }
 
-    scg::DevBuf<double> x, so0, so1, cfl;
+    scg::DevBuf<double> x, geo, so0, so1, cfl;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
 };
@@ -464,6 +548,11 @@ int scg_st_march(scg_st * h, int alpha, int64_t steps)
 int scg_st_sync(scg_st * h)
 {
     return scg::guarded([&] { h->c->sync(); });
+}
+
+int scg_st_stream(const scg_st * h, void ** out)
+{
+    return scg::guarded([&] { *out = h->c->stream; });
 }
 
 } // extern "C"

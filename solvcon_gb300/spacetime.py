@@ -32,6 +32,7 @@ lib = _lib.bind_more({
                   ctypes.c_int),
     "scg_st_march": ([_vp, ctypes.c_int, ctypes.c_int64], ctypes.c_int),
     "scg_st_sync": ([_vp], ctypes.c_int),
+    "scg_st_stream": ([_vp, _vp], ctypes.c_int),
 })
 
 BOUND_COUNT = 2
