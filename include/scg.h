@@ -90,6 +90,21 @@ int scg_mesh_bc(const scg_mesh * mesh, int64_t ibc, char * buf, int64_t buflen, 
 int scg_mesh_build_boundary(scg_mesh * mesh);
 /* build_ghost: StaticMesh_boundary.cpp:185-240. */
 int scg_mesh_build_ghost(scg_mesh * mesh);
+/* A mesh read from a Gmsh MSH 2.2 ASCII file's contents (nbyte bytes at
+ * data): inout::Gmsh(data).to_block() (cpp/solvcon/inout/gmsh.cpp:14-118,
+ * gmsh.hpp:70-285).  The elements of the highest dimension become the cells,
+ * every node is kept, and the mesh comes back with build_interior,
+ * build_boundary and build_ghost done.  A malformed file (wrong version,
+ * missing or out-of-order sections) gives SCG_EINVAL; a node id out of range
+ * SCG_ERANGE.  Free with scg_mesh_destroy. */
+int scg_mesh_from_gmsh(const char * data, int64_t nbyte, scg_mesh ** out);
+/* A mesh of hexahedra read from a Plot3D multi-block ASCII grid file's
+ * contents: inout::Plot3d(data).to_block() (cpp/solvcon/inout/plot3d.cpp:
+ * 14-155).  One hexahedron per grid cell of every block, blocks share no
+ * nodes, and the mesh comes back with build_interior, build_boundary and
+ * build_ghost done.  A malformed file gives SCG_EINVAL.  Free with
+ * scg_mesh_destroy. */
+int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
 
 /* ------------------------------------------------------------------------
  * Multi-dimensional Euler CESE core on the GPU.

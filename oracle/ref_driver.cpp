@@ -11,6 +11,8 @@
  * last failure is available from ref_last_error().
  */
 
+#include <solvcon/inout/gmsh.hpp>
+#include <solvcon/inout/plot3d.hpp>
 #include <solvcon/mesh/mesh.hpp>
 #include <solvcon/multidim/multidim.hpp>
 #include <solvcon/onedim/Euler1DCore.hpp>
@@ -119,6 +121,24 @@ int ref_mesh_add_bc(void * h, char const * name, int const * faces, int n)
                  {
         std::vector<int32_t> f(faces, faces + n);
         static_cast<RefMesh *>(h)->mesh->add_bc(std::string(name), f); });
+}
+
+// inout::Gmsh(data).to_block(): the mesh of a Gmsh MSH file's contents.
+int ref_gmsh_load(char const * data, long long nbyte, void ** out)
+{
+    return guard([&]
+                 {
+        solvcon::inout::Gmsh g(std::string(data, static_cast<size_t>(nbyte)));
+        *out = new RefMesh{g.to_block()}; });
+}
+
+// inout::Plot3d(data).to_block(): the mesh of a Plot3D file's contents.
+int ref_plot3d_load(char const * data, long long nbyte, void ** out)
+{
+    return guard([&]
+                 {
+        solvcon::inout::Plot3d p(std::string(data, static_cast<size_t>(nbyte)));
+        *out = new RefMesh{p.to_block()}; });
 }
 
 // stage: 0 build_interior(do_metric=true, do_edge=true), 1 build_boundary,

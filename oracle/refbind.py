@@ -69,6 +69,29 @@ class RefMesh:
             _check(lib().ref_mesh_build(h, 1))
             _check(lib().ref_mesh_build(h, 2))
 
+    @classmethod
+    def from_gmsh(cls, data):
+        """The reference's Gmsh reader on a MSH file's contents."""
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        lib().ref_gmsh_load.argtypes = [ctypes.c_char_p, ctypes.c_longlong,
+                                        ctypes.c_void_p]
+        _check(lib().ref_gmsh_load(bytes(data), len(data), ctypes.byref(h)))
+        self.h = h
+        return self
+
+    @classmethod
+    def from_plot3d(cls, data):
+        """The reference's Plot3D reader on a file's contents."""
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        lib().ref_plot3d_load.argtypes = [ctypes.c_char_p,
+                                          ctypes.c_longlong, ctypes.c_void_p]
+        _check(lib().ref_plot3d_load(bytes(data), len(data),
+                                     ctypes.byref(h)))
+        self.h = h
+        return self
+
     def sizes(self):
         out = (ctypes.c_longlong * 10)()
         _check(lib().ref_mesh_sizes(self.h, out))

@@ -42,6 +42,10 @@ _SIGS = {
                     ctypes.c_int),
     "scg_mesh_build_boundary": ([_vp], ctypes.c_int),
     "scg_mesh_build_ghost": ([_vp], ctypes.c_int),
+    "scg_mesh_from_gmsh": ([ctypes.c_char_p, ctypes.c_int64, _vp],
+                           ctypes.c_int),
+    "scg_mesh_from_plot3d": ([ctypes.c_char_p, ctypes.c_int64, _vp],
+                             ctypes.c_int),
     "scg_euler_create": ([_vp, ctypes.c_double, ctypes.c_int, _vp],
                          ctypes.c_int),
     "scg_euler_destroy": ([_vp], ctypes.c_int),

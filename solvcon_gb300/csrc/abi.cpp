@@ -28,10 +28,6 @@ std::string const & last_error() { return t_last_error; }
 
 } // namespace scg
 
-struct scg_mesh
-{
-    scg::HostMesh m;
-};
 
 using scg::guarded;
 

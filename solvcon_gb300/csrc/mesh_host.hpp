@@ -118,3 +118,9 @@ private:
 };
 
 } // namespace scg
+
+// The opaque handle behind scg_mesh* in include/scg.h.
+struct scg_mesh
+{
+    scg::HostMesh m;
+};

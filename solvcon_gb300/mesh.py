@@ -17,7 +17,7 @@ from . import _lib
 from ._lib import check, lib, ptr
 from .buffer import SimpleArray
 
-__all__ = ["StaticMesh", "StaticMeshBc"]
+__all__ = ["StaticMesh", "StaticMeshBc", "Gmsh", "Plot3d"]
 
 _ARRAYS = ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol", "fctpn",
            "cltpn", "clgrp", "fcnds", "fccls", "clnds", "clfcs", "ednds",
@@ -60,6 +60,13 @@ class StaticMesh:
         check(lib.scg_mesh_create(int(ndim), int(nnode), int(nface),
                                   int(ncell), ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def _adopt(cls, handle):
+        """Wrap a native scg_mesh handle (the wrapper destroys it)."""
+        self = cls.__new__(cls)
+        self._h = handle
+        return self
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -164,3 +171,55 @@ for _i, _name in enumerate(_ARRAYS):
     setattr(StaticMesh, _name, _make_prop(_i))
 del _i, _name, _make_prop
 _ = _lib
+
+
+class Gmsh:
+    """Gmsh MSH 2.2 (ASCII) reader (cpp/solvcon/inout/gmsh.hpp:70-285,
+    wrapped as ``solvcon.Gmsh``): ``Gmsh(data).to_block()`` gives the
+    :class:`StaticMesh` of the file's highest-dimension elements, with the
+    interior, boundary and ghost tables built.  ``data`` is the file's
+    contents (bytes or str); the parsing is native."""
+
+    def __init__(self, data):
+        if isinstance(data, str):
+            data = data.encode()
+        self._data = bytes(data)
+        # Parse now, as the reference's constructor does, so a malformed
+        # file raises here.
+        self._mesh = self._read()
+
+    def _read(self):
+        h = ctypes.c_void_p()
+        check(lib.scg_mesh_from_gmsh(self._data, len(self._data),
+                                     ctypes.byref(h)))
+        return StaticMesh._adopt(h)
+
+    def to_block(self):
+        """The mesh (a new StaticMesh on each call)."""
+        mesh, self._mesh = self._mesh, None
+        return mesh if mesh is not None else self._read()
+
+
+class Plot3d:
+    """Plot3D multi-block ASCII grid reader (cpp/solvcon/inout/plot3d.hpp:
+    22-80, wrapped as ``solvcon.core.Plot3d``): ``Plot3d(data).to_block()``
+    gives the :class:`StaticMesh` of one hexahedron per grid cell, with the
+    interior, boundary and ghost tables built.  The parsing is native."""
+
+    def __init__(self, data):
+        if isinstance(data, str):
+            data = data.encode()
+        self._data = bytes(data)
+        self._mesh = self._read()
+
+    def _read(self):
+        h = ctypes.c_void_p()
+        check(lib.scg_mesh_from_plot3d(self._data, len(self._data),
+                                       ctypes.byref(h)))
+        return StaticMesh._adopt(h)
+
+    def to_block(self):
+        """The mesh (a new StaticMesh on each call)."""
+        mesh, self._mesh = self._mesh, None
+        return mesh if mesh is not None else self._read()
+

@@ -8,9 +8,14 @@ seeded cases and stores its outputs as .npz files:
   build_boundary and build_ghost (the mesh builder's golden vectors);
 * march_<case>.npz -- initial state, boundary setup and the EulerCore arrays
   after a number of march steps (the march's golden vectors);
-* e1d_sod.npz -- the Euler1DCore Sod tube after march_alpha2.
+* e1d_sod.npz -- the Euler1DCore Sod tube after march_alpha2;
+* gmsh_<case>.npz -- a Gmsh MSH 2.2 file written by meshgen.to_gmsh (its text
+  in "msh") and every StaticMesh table the reference's Gmsh reader builds
+  from it;
+* plot3d_<case>.npz -- the same for Plot3D grid files (text in "p3d").
 
-Usage: python tests/golden/make_golden.py   (needs oracle/_ref built)
+Usage: python tests/golden/make_golden.py [gmsh]   (needs oracle/_ref built;
+"gmsh" / "plot3d" write only that reader's fixtures)
 """
 
 import os
@@ -121,7 +126,120 @@ def e1d_golden():
     np.savez_compressed(os.path.join(HERE, "e1d_sod.npz"), **out)
 
 
+def gmsh_cases():
+    """Gmsh files of the reader's fixtures: (text, ndim, ndcrd, cltpn, clnds)
+    where the last three are the mesh the file describes (None when the file
+    carries nodes no cell uses)."""
+    out = {}
+    # The reference test's triangle fan (tests/test_gmsh.py:19-40), with a
+    # boundary line, a point and a physical name besides the cells.
+    x = [(0.0, 0.0), (-1.0, -1.0), (1.0, -1.0), (0.0, 1.0)]
+    t = [4, 4, 4]
+    c = [(3, 0, 1, 2), (3, 0, 2, 3), (3, 0, 3, 1)]
+    txt = meshgen.to_gmsh(2, x, t, c, lower=[(15, 7, [1]), (1, 5, [1, 2])],
+                          names=[(1, 5, "wall"), (2, 1, "fluid")])
+    out["tri3"] = (txt, 2, x, t, c)
+    # Quads with every third one split into two triangles, boundary lines.
+    xq, tq, cq = meshgen.quad_square(6, 0.15, seed=21)
+    cells, types = [], []
+    for k, row in enumerate(cq):
+        a, b, cc, d = (int(v) for v in row[1:5])
+        if k % 3 == 0:
+            cells += [(3, a, b, cc), (3, a, cc, d)]
+            types += [4, 4]
+        else:
+            cells.append((4, a, b, cc, d))
+            types.append(3)
+    clnds = np.full((len(cells), 5), -1, dtype="int32")
+    for k, row in enumerate(cells):
+        clnds[k, :len(row)] = row
+    lines = [(1, 3, [i, i + 1]) for i in range(6)]
+    txt = meshgen.to_gmsh(2, xq, types, clnds, lower=lines,
+                          names=[(1, 3, "bottom")])
+    out["mixed2d"] = (txt, 2, xq, types, clnds)
+    # The same with some triangles written as 6-node triangles: their
+    # mid-edge nodes are in $Nodes but in no cell.
+    tri = [k for k, tp in enumerate(types) if tp == 4][::2]
+    txt = meshgen.to_gmsh(2, xq, types, clnds, second_order=tri)
+    out["order2"] = (txt, 2, None, None, None)
+    # 3D: a hexahedral block, a prism slab beside it, a pyramid and a
+    # tetrahedron (four components, every 3D type and the prism's Gmsh
+    # corner order).
+    xh, th, ch = meshgen.hex_cube(2, 0.1, seed=22)
+    xp, tp, cp = meshgen.prism_slab(2, 1, 0.1, seed=23)
+    xp = xp + np.array([1.5, 0.0, 0.0])
+    xy = np.array([(3.0, 0, 0), (4, 0, 0), (4, 1, 0), (3, 1, 0),
+                   (3.5, 0.5, 1), (5, 0, 0), (6, 0, 0), (5, 1, 0),
+                   (5, 0, 1)], dtype="float64")
+    nh, npr = len(xh), len(xp)
+    x3 = np.vstack([xh, xp, xy])
+    t3 = list(th) + list(tp) + [8, 6]
+    c3 = np.full((len(t3), 9), -1, dtype="int32")
+    c3[:len(th), :9] = ch[:, :9]
+    c3[len(th):len(th) + len(tp), :7] = cp[:, :7] + np.array([0] + [nh] * 6)
+    base = nh + npr
+    c3[-2, :6] = [5] + [base + i for i in range(5)]
+    c3[-1, :5] = [4] + [base + 5 + i for i in range(4)]
+    txt = meshgen.to_gmsh(3, x3, t3, c3)
+    out["mixed3d"] = (txt, 3, x3, t3, c3)
+    return out
+
+
+def plot3d_cases():
+    """Plot3D files of the reader's fixtures: a jittered single block, and
+    three blocks of different shapes side by side."""
+    rng = np.random.Generator(np.random.PCG64(31))
+
+    def block(ni, nj, nk, x0, jitter):
+        g = np.stack(np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni),
+                                 indexing="ij"), axis=-1)[..., ::-1]
+        g = g.astype("float64") + rng.uniform(-jitter, jitter, g.shape)
+        g[..., 0] += x0
+        return g
+    return {"cube": meshgen.to_plot3d([block(4, 3, 3, 0.0, 0.2)]),
+            "blocks": meshgen.to_plot3d([block(3, 2, 2, 0.0, 0.1),
+                                         block(2, 3, 2, 5.0, 0.1),
+                                         block(2, 2, 4, 10.0, 0.0)])}
+
+
+def mesh_golden_from(name, r, extra):
+    out = dict(extra)
+    sizes = r.sizes()
+    out["sizes"] = np.array([sizes[k] for k in
+                             ("ndim", "nnode", "nface", "ncell", "nbound",
+                              "ngstnode", "ngstface", "ngstcell", "nedge",
+                              "nbcs")], dtype="int64")
+    for a in MESH_ARRAYS:
+        out[a] = r.array(a)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def gmsh_golden(name, text):
+    r = rb.RefMesh.from_gmsh(text.encode())
+    out = {"msh": np.array(text)}
+    sizes = r.sizes()
+    out["sizes"] = np.array([sizes[k] for k in
+                             ("ndim", "nnode", "nface", "ncell", "nbound",
+                              "ngstnode", "ngstface", "ngstcell", "nedge",
+                              "nbcs")], dtype="int64")
+    for a in MESH_ARRAYS:
+        out[a] = r.array(a)
+    np.savez_compressed(os.path.join(HERE, "gmsh_%s.npz" % name), **out)
+
+
 def main():
+    if sys.argv[1:] == ["gmsh"]:
+        for name, case in gmsh_cases().items():
+            gmsh_golden(name, case[0])
+        print("gmsh fixtures written to", HERE)
+        return
+    if sys.argv[1:] == ["plot3d"]:
+        for name, text in plot3d_cases().items():
+            mesh_golden_from("plot3d_" + name,
+                             rb.RefMesh.from_plot3d(text.encode()),
+                             {"p3d": np.array(text)})
+        print("plot3d fixtures written to", HERE)
+        return
     cases = fixture_cases()
     meshes = {k: mesh_golden(k, *v) for k, v in cases.items()}
     for name, kind in (("tri12", 1), ("quad8", 0), ("tet3", 1)):
@@ -133,6 +251,12 @@ def main():
                                      radius=0.35)
         march_golden(name, mesh, nd, state, kind, 2e-3, 6)
     e1d_golden()
+    for name, case in gmsh_cases().items():
+        gmsh_golden(name, case[0])
+    for name, text in plot3d_cases().items():
+        mesh_golden_from("plot3d_" + name,
+                         rb.RefMesh.from_plot3d(text.encode()),
+                         {"p3d": np.array(text)})
     print("golden fixtures written to", HERE)
 
 
