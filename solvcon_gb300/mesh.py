@@ -29,7 +29,9 @@ class StaticMeshBc:
 
     def __init__(self, name, facn):
         self.name = name
-        self.facn = facn
+        # [nbound, 3] face table as a SimpleArray (facn.ndarray is the
+        # numpy array, as in the reference's BC object).
+        self.facn = SimpleArray(lambda: facn)
 
     @property
     def nbound(self):
