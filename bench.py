@@ -52,7 +52,7 @@ ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
 # fused_substep_{tri2d_fp64,tri2d_fp32,tet3d_fp64}.md); absent until captured.  The FP64
 # records carry a primitive cache (192 B instead of 128 B), which trades
 # DRAM bytes, idle in the FP64-bound march, for FP64 operations.
-NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 770.2, ("tri2d", "fp32"): 321.8,
+NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 770.2, ("tri2d", "fp32"): 270.2,
                         ("tet3d", "fp64"): 1337.3}
 NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1195.6, ("tet3d", "fp64"): 2717.4}
 

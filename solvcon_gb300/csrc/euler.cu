@@ -554,7 +554,7 @@ class EulerCoreImpl : public EulerCoreBase
 public:
     static constexpr int NEQ = ND + 2;
     static constexpr int RS = Rec<ND, R>::RS;
-    static constexpr int KF = Dim<ND>::KF;
+    static constexpr int KF = Geo<ND, G>::KF;
 
     EulerCoreImpl(HostMesh const & mesh, double dt, int prec)
     {

@@ -51,17 +51,31 @@ struct Dim
     static constexpr int RS = (ND == 2) ? 16 : 32; // record stride in reals
     static constexpr int OT = NEQ;                 // so0t offset
     static constexpr int O1 = 2 * NEQ;             // so1 offset
-    // Face geometry components: bvol, dB[ND], Nh[ND], Mh[ND][ND], P[ND], Q[ND], R[ND].
+    // Cell geometry components: 1/cevol[0], hdt/dist.
+    static constexpr int KC = 2;
+};
+
+// Per-face geometry components, stored as G: bvol, dB[ND] = x_BCE - x_nbr,
+// Nh[ND], Mh[ND][ND], then either the gradient-element displacements P[ND],
+// Q[ND], R[ND] (FP64 geometry) or mid[ND] = x_BCE - x_cell (FP32 geometry).
+// P, Q and R follow from dB and mid with means over the cell's faces:
+//   P = mid - mean(mid),  Q = mean(dB) - dB,  R = dB - mean(mid),
+// which the memory-bound FP32 march forms in registers for 4 (2D) or 6 (3D)
+// fewer stored values per face; the FP64 march, bound by its FP64 pipe,
+// reads them.
+template <int ND, typename G>
+struct Geo
+{
+    static constexpr bool MID = sizeof(G) == 4;
     static constexpr int K_BVOL = 0;
     static constexpr int K_DB = 1;
     static constexpr int K_NH = 1 + ND;
     static constexpr int K_MH = 1 + 2 * ND;
-    static constexpr int K_P = 1 + 2 * ND + ND * ND;
+    static constexpr int K_P = 1 + 2 * ND + ND * ND; // FP64 geometry
     static constexpr int K_Q = K_P + ND;
     static constexpr int K_R = K_Q + ND;
-    static constexpr int KF = K_R + ND;
-    // Cell geometry components: 1/cevol[0], hdt/dist.
-    static constexpr int KC = 2;
+    static constexpr int K_MID = K_P; // FP32 geometry
+    static constexpr int KF = MID ? K_MID + ND : K_R + ND;
 };
 
 // Record layout per dimension and state precision.

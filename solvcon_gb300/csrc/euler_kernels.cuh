@@ -120,7 +120,7 @@ __device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0
 template <int ND, typename R, typename G>
 __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t icl)
 {
-    return R(ldg(a.fgeo + (static_cast<int64_t>(f) * Dim<ND>::KF + k) * a.ncell + icl));
+    return R(ldg(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
 }
 
 // ---------------------------------------------------------------------------
@@ -135,7 +135,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
     constexpr int NFC = CellT<CT>::NFC;
-    using D = Dim<ND>;
+    using D = Geo<ND, G>;
     using RC = Rec<ND, R>;
     constexpr bool USE = CACHE && RC::PRIM;
     Acc<R> acc[NEQ];
@@ -266,12 +266,69 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     constexpr int NEQ = ND + 2;
     constexpr int NFC = CellT<CT>::NFC;
     constexpr int NFGE = CellT<CT>::NFGE;
-    using D = Dim<ND>;
+    using D = Geo<ND, G>;
 
     R const acfl = fabs(cflc);
     R const sgm0 = a.sigma0 / acfl;
     R const tau = a.taumin + acfl * a.tauscale;
     R const ofg1 = R(1) / R(NFGE);
+
+    // The gradient-element displacements P, Q, R of every face.
+    R gp[NFC][ND], gq[NFC][ND], gr[NFC][ND];
+    if constexpr (D::MID)
+    {
+        R mm[ND], mb[ND];
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            mm[d] = R(0);
+            mb[d] = R(0);
+        }
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                gp[f][d] = fg<ND>(a, f, D::K_MID + d, icl);
+                gr[f][d] = fg<ND>(a, f, D::K_DB + d, icl);
+                mm[d] += gp[f][d];
+                mb[d] += gr[f][d];
+            }
+        }
+        R const inv = R(1) / R(NFC);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            mm[d] *= inv;
+            mb[d] *= inv;
+        }
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                gq[f][d] = mb[d] - gr[f][d];
+                gp[f][d] -= mm[d];
+                gr[f][d] -= mm[d];
+            }
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                gp[f][d] = fg<ND>(a, f, D::K_P + d, icl);
+                gq[f][d] = fg<ND>(a, f, D::K_Q + d, icl);
+                gr[f][d] = fg<ND>(a, f, D::K_R + d, icl);
+            }
+        }
+    }
 
     // Gradient-evaluation displacements: idis = dst - delta, dst = P + tau Q.
     R idis[NFC][ND];
@@ -281,7 +338,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
-            idis[f][d] = fg<ND>(a, f, D::K_P + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl);
+            idis[f][d] = gp[f][d] + tau * gq[f][d];
         }
     }
     R delta[ND];
@@ -343,7 +400,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
-            jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+            jd[d] = gr[f][d] + tau * gq[f][d] - delta[d];
         }
 #pragma unroll
         for (int i = 0; i < NEQ; ++i)

@@ -200,7 +200,7 @@ __global__ void k_compact(MeshView m, double const * cevol, double const * cecnd
                           double const * sfnml, double hdt, int nslot, G * fgeo, G * cgeo, int32_t * nbr,
                           int8_t * ctype)
 {
-    using D = Dim<ND>;
+    using D = Geo<ND, G>;
     int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t const nc = m.ncell;
     if (icl >= nc)
@@ -287,9 +287,16 @@ __global__ void k_compact(MeshView m, double const * cevol, double const * cecnd
     {
         for (int d = 0; d < ND; ++d)
         {
-            put(f, D::K_P + d, mid[f][d] - A[d]);
-            put(f, D::K_Q + d, ee[f][d] - B[d]);
-            put(f, D::K_R + d, -(A[d] + ee[f][d]));
+            if constexpr (D::MID)
+            {
+                put(f, D::K_MID + d, mid[f][d]);
+            }
+            else
+            {
+                put(f, D::K_P + d, mid[f][d] - A[d]);
+                put(f, D::K_Q + d, ee[f][d] - B[d]);
+                put(f, D::K_R + d, -(A[d] + ee[f][d]));
+            }
         }
     }
     for (int f = clnfc; f < nslot; ++f)
