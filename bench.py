@@ -904,6 +904,54 @@ def run_accuracy(args, world, rank, dist):
     print(json.dumps(out), flush=True)
 
 
+def run_meshbuild(args, world, rank, dist):
+    """Time to first step of the 3D workload's mesh (160^3 x 6 tetrahedra by
+    default): StaticMesh build_interior + build_boundary + build_ghost on the
+    host and with build_interior on the GPU (tables compared), then the GPU
+    core's set-up (upload, prepare_ce, compaction) on the built mesh.  The
+    node and cell arrays are generated before the clock starts."""
+    import solvcon_gb300 as sg
+    from solvcon_gb300 import meshgen
+    if rank != 0:
+        return
+    nside = args.nside or 160
+    x, t, c = meshgen.tet_cube(nside, 0.15, 2026)
+    out = {"metric": "mesh build s", "unit": "s", "higher_is_better": False,
+           "config": {"workload": "tet3d mesh, %d^3 x 6 = %d tetrahedra" %
+                      (nside, len(t))}, "data": "synthetic"}
+    meshes = {}
+    for name, device in (("host", False), ("device", True)):
+        t0 = time.perf_counter()
+        m = sg.StaticMesh(ndim=3, nnode=len(x), nface=0, ncell=len(t))
+        m.ndcrd[:, :] = x
+        m.cltpn[:] = t
+        m.clnds[:, :c.shape[1]] = c
+        t1 = time.perf_counter()
+        m.build_interior(do_metric=True, build_edge=False, device=device)
+        t2 = time.perf_counter()
+        m.build_boundary()
+        m.build_ghost()
+        t3 = time.perf_counter()
+        out[name] = {"fill_s": t1 - t0, "build_interior_s": t2 - t1,
+                     "boundary_ghost_s": t3 - t2, "total_s": t3 - t0}
+        meshes[name] = m
+    same = all(np.array_equal(np.asarray(getattr(meshes["host"], a).ndarray),
+                              np.asarray(getattr(meshes["device"], a).ndarray))
+               for a in ("fccls", "fcnds", "clfcs", "fccnd", "fcnml", "clvol",
+                         "clcnd", "ndcrd"))
+    out["tables_equal"] = bool(same)
+    m = meshes.pop("device")
+    meshes.clear()
+    t0 = time.perf_counter()
+    core = sg.EulerCore(m, 1e-4, precision="fp32")
+    core.sync()
+    out["core_setup_s"] = time.perf_counter() - t0
+    out["value"] = out["device"]["total_s"]
+    out["speedup_build_interior"] = (out["host"]["build_interior_s"] /
+                                     out["device"]["build_interior_s"])
+    print(json.dumps(out), flush=True)
+
+
 def _desc(w):
     if w["ndim"] == 2:
         return ("2D Euler, unit square %dx%d quads x 2 triangles = %d cells, "
@@ -923,7 +971,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tri2d",
                     choices=sorted(WORKLOADS) + ["batch", "serve",
-                                                 "accuracy"] +
+                                                 "accuracy", "meshbuild"] +
                     sorted(LINE_WORKLOADS))
     ap.add_argument("--precision", default=None,
                     choices=["fp64", "fp32", "fp32-geom64"])
@@ -944,11 +992,12 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         return
-    if args.workload in ("batch", "serve", "accuracy") or (
+    if args.workload in ("batch", "serve", "accuracy", "meshbuild") or (
             args.workload in LINE_WORKLOADS and args.impl != "reference"):
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
         import solvcon_gb300  # noqa: F401
         {"batch": run_batch, "serve": run_serve, "accuracy": run_accuracy,
+         "meshbuild": run_meshbuild,
          "tube1d": run_line, "spacetime": run_line}[args.workload](
              args, world, rank, dist)
         if dist is not None:

@@ -81,6 +81,15 @@ int scg_mesh_array(scg_mesh * mesh, int which, void ** data, int64_t * shape, in
 int scg_mesh_build_interior(scg_mesh * mesh, int do_metric, int do_edge);
 /* build_edge: StaticMesh_interior.cpp:545. */
 int scg_mesh_build_edge(scg_mesh * mesh);
+/* build_interior on the GPU: face extraction, de-duplication and numbering,
+ * face-cell relations and metrics in device kernels, the tables copied back;
+ * every table equals scg_mesh_build_interior's entry for entry
+ * (StaticMesh_interior.cpp:332-977 restated per face and per cell).  Needs a
+ * GPU and a mesh without ghost layer whose cells all have the mesh's
+ * dimension (others go to the host builder or give SCG_EINVAL). */
+int scg_mesh_build_interior_device(scg_mesh * mesh, int do_metric, int do_edge);
+/* Number of CUDA devices visible (0 without a driver or a GPU). */
+int scg_device_count(int * out);
 /* add_bc(name, faces): StaticMesh_boundary.cpp:68-78. */
 int scg_mesh_add_bc(scg_mesh * mesh, const char * name, const int32_t * faces, int64_t nface);
 /* Name and facn table [nbound][3] of boundary group ibc (StaticMesh.hpp:159-251);

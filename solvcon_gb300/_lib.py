@@ -42,6 +42,9 @@ _SIGS = {
                     ctypes.c_int),
     "scg_mesh_build_boundary": ([_vp], ctypes.c_int),
     "scg_mesh_build_ghost": ([_vp], ctypes.c_int),
+    "scg_mesh_build_interior_device": ([_vp, ctypes.c_int, ctypes.c_int],
+                                       ctypes.c_int),
+    "scg_device_count": ([_vp], ctypes.c_int),
     "scg_mesh_from_gmsh": ([ctypes.c_char_p, ctypes.c_int64, _vp],
                            ctypes.c_int),
     "scg_mesh_from_plot3d": ([ctypes.c_char_p, ctypes.c_int64, _vp],

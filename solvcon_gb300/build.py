@@ -47,7 +47,7 @@ def headers():
 # whether a half step runs as one fused kernel or as separate so0/cfl/so1
 # kernels (the reference tests its fine-grained and one-call marches for
 # equality); without contraction every instantiation rounds the same way.
-FILE_FLAGS = {"spacetime.cu": ["--fmad=false"]}
+FILE_FLAGS = {"spacetime.cu": ["--fmad=false"], "mesh_device.cu": ["--fmad=false"]}
 
 
 def _compile(src, extra):

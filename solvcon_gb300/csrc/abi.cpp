@@ -132,6 +132,21 @@ int scg_mesh_build_interior(scg_mesh * mesh, int do_metric, int do_edge)
     return guarded([&] { need(mesh, "scg_mesh_build_interior")->m.build_interior(do_metric != 0, do_edge != 0); });
 }
 
+int scg_mesh_build_interior_device(scg_mesh * mesh, int do_metric, int do_edge)
+{
+    return guarded([&]
+                   { need(mesh, "scg_mesh_build_interior_device")->m.build_interior_device(do_metric != 0, do_edge != 0); });
+}
+
+int scg_device_count(int * out)
+{
+    return guarded([&] {
+        int n = 0;
+        *out = cudaGetDeviceCount(&n) == cudaSuccess ? n : 0;
+        cudaGetLastError();
+    });
+}
+
 int scg_mesh_build_edge(scg_mesh * mesh)
 {
     return guarded([&] { need(mesh, "scg_mesh_build_edge")->m.build_edge(); });

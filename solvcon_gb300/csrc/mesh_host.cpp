@@ -6,6 +6,7 @@
  */
 
 #include "mesh_host.hpp"
+#include "mesh_cells.hpp"
 
 #include <algorithm>
 #include <array>
@@ -18,55 +19,6 @@
 
 namespace scg
 {
-
-namespace
-{
-
-struct FaceDef
-{
-    int32_t type;       // face cell type
-    int nnd;            // nodes of the face
-    std::array<int, 4> pos; // 1-based positions into the cell's node list
-};
-
-struct CellFaces
-{
-    int nface;
-    std::array<FaceDef, CLMFC> f;
-};
-
-// Face-to-node tables of each cell type: the node order of every face as the
-// reference's FaceBuilder::add_* emits it (StaticMesh_interior.cpp:26-330).
-CellFaces cell_faces(int32_t type)
-{
-    switch (type)
-    {
-    case CT_QUAD:
-        return {4, {{{CT_LINE, 2, {1, 2}}, {CT_LINE, 2, {2, 3}}, {CT_LINE, 2, {3, 4}}, {CT_LINE, 2, {4, 1}}}}};
-    case CT_TRIANGLE:
-        return {3, {{{CT_LINE, 2, {1, 2}}, {CT_LINE, 2, {2, 3}}, {CT_LINE, 2, {3, 1}}}}};
-    case CT_HEX:
-        return {6, {{{CT_QUAD, 4, {1, 4, 3, 2}}, {CT_QUAD, 4, {2, 3, 7, 6}}, {CT_QUAD, 4, {5, 6, 7, 8}},
-                     {CT_QUAD, 4, {1, 5, 8, 4}}, {CT_QUAD, 4, {1, 2, 6, 5}}, {CT_QUAD, 4, {3, 4, 8, 7}}}}};
-    case CT_TET:
-        return {4, {{{CT_TRIANGLE, 3, {1, 3, 2}}, {CT_TRIANGLE, 3, {1, 2, 4}}, {CT_TRIANGLE, 3, {1, 4, 3}},
-                     {CT_TRIANGLE, 3, {2, 3, 4}}}}};
-    case CT_PRISM:
-        return {5, {{{CT_TRIANGLE, 3, {1, 2, 3}}, {CT_TRIANGLE, 3, {4, 6, 5}}, {CT_QUAD, 4, {1, 4, 5, 2}},
-                     {CT_QUAD, 4, {1, 3, 6, 4}}, {CT_QUAD, 4, {2, 5, 6, 3}}}}};
-    case CT_PYRAMID:
-        return {5, {{{CT_TRIANGLE, 3, {1, 5, 4}}, {CT_TRIANGLE, 3, {2, 5, 1}}, {CT_TRIANGLE, 3, {3, 5, 2}},
-                     {CT_TRIANGLE, 3, {4, 5, 3}}, {CT_QUAD, 4, {1, 4, 3, 2}}}}};
-    case CT_LINE:
-        return {2, {{{CT_POINT, 1, {1}}, {CT_POINT, 1, {2}}}}};
-    case CT_POINT:
-        return {1, {{{CT_NONE, 0, {1}}}}};
-    default:
-        return {0, {}};
-    }
-}
-
-} // namespace
 
 int cell_nface(int32_t type) { return cell_faces(type).nface; }
 
@@ -135,7 +87,7 @@ void HostMesh::build_interior(bool do_metric, bool do_edge)
 // 331-528): populate every cell's faces, find duplicates through a
 // node-to-face table keyed on each face's first node, compact, and record the
 // two cells of each face in ascending cell order.
-void HostMesh::build_faces_from_cells()
+void HostMesh::validate_cells() const
 {
     for (int64_t icl = 0; icl < ncell; ++icl)
     {
@@ -155,6 +107,11 @@ void HostMesh::build_faces_from_cells()
             }
         }
     }
+}
+
+void HostMesh::build_faces_from_cells()
+{
+    validate_cells();
 
     int64_t mface = 0;
     for (int64_t icl = 0; icl < ncell; ++icl)
@@ -667,6 +624,10 @@ void HostMesh::remake(Table<T> & t, int64_t ngst, int64_t nb, int64_t w, T init)
         m_retired_int.push_back(std::move(t.buf));
     t.make(ngst, nb, w, init);
 }
+
+// Used by the device builder (mesh_device.cu) as well.
+template void HostMesh::remake<int32_t>(Table<int32_t> &, int64_t, int64_t, int64_t, int32_t);
+template void HostMesh::remake<double>(Table<double> &, int64_t, int64_t, int64_t, double);
 
 template <typename T>
 void HostMesh::regrow(Table<T> & t, int64_t ngst, T init)

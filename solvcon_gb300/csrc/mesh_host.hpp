@@ -81,6 +81,10 @@ public:
 
     // StaticMesh::build_interior (StaticMesh.hpp:363-374).
     void build_interior(bool do_metric, bool do_edge);
+    // The same tables built on the GPU (face extraction, de-duplication and
+    // numbering, face-cell relations, metrics; mesh_device.cu), entry for
+    // entry equal to build_interior's; edges, when asked for, on the host.
+    void build_interior_device(bool do_metric, bool do_edge);
     void build_edge();
     // StaticMesh::add_bc (StaticMesh_boundary.cpp:14-78).
     void add_bc(std::string const & name, std::vector<int32_t> const & faces);
@@ -112,6 +116,7 @@ private:
     std::vector<std::vector<double>> m_retired_real;
     std::vector<std::vector<int32_t>> m_retired_int;
 
+    void validate_cells() const;
     void build_faces_from_cells();
     void calc_metric();
     void fill_ghost();

@@ -24,6 +24,18 @@ _ARRAYS = ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol", "fctpn",
            "bndfcs")
 
 
+_GPUS = None
+
+
+def _gpu_count():
+    global _GPUS
+    if _GPUS is None:
+        n = ctypes.c_int()
+        check(lib.scg_device_count(ctypes.byref(n)))
+        _GPUS = n.value
+    return _GPUS
+
+
 class StaticMeshBc:
     """A boundary group of a :class:`StaticMesh` (StaticMesh.hpp:159-251)."""
 
@@ -101,9 +113,21 @@ class StaticMesh:
 
     # -- builds -------------------------------------------------------------
 
-    def build_interior(self, do_metric=True, build_edge=True):
-        check(lib.scg_mesh_build_interior(self._h, int(bool(do_metric)),
-                                          int(bool(build_edge))))
+    #: Meshes at least this large build their interior on the GPU when one
+    #: is present (``build_interior(device=None)``).
+    DEVICE_BUILD_CELLS = 65536
+
+    def build_interior(self, do_metric=True, build_edge=True, device=None):
+        """Faces, face-cell relations and (with ``do_metric``) the metrics
+        (StaticMesh::build_interior).  ``device=True`` builds them on the GPU,
+        ``False`` on the host; ``None`` picks the GPU for meshes of at least
+        :attr:`DEVICE_BUILD_CELLS` cells when one is present.  Both give the
+        same tables entry for entry."""
+        if device is None:
+            device = self.ncell >= self.DEVICE_BUILD_CELLS and _gpu_count() > 0
+        fn = lib.scg_mesh_build_interior_device if device else \
+            lib.scg_mesh_build_interior
+        check(fn(self._h, int(bool(do_metric)), int(bool(build_edge))))
 
     def build_edge(self):
         check(lib.scg_mesh_build_edge(self._h))

@@ -35,7 +35,10 @@ def _build(g):
 @pytest.mark.parametrize("case", CASES)
 def test_mesh_matches_reference_golden(case):
     g = golden("mesh_" + case)
-    m = _build(g)
+    _same_as_golden(_build(g), g)
+
+
+def _same_as_golden(m, g):
     assert [getattr(m, k) for k in SIZES] == list(g["sizes"])
     for name in INT_ARRAYS:
         got = np.asarray(getattr(m, name).ndarray).ravel()
