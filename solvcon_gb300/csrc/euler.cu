@@ -1128,7 +1128,14 @@ public:
         constexpr int SIMPLEX = (ND == 2) ? CT_TRIANGLE : CT_TET;
         if (single_ct == SIMPLEX)
         {
-            k_fused<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            if constexpr (ND == 3 && sizeof(R) == 4)
+            {
+                k_fused_5<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            }
+            else
+            {
+                k_fused<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            }
         }
         else
         {

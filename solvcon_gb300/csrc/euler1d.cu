@@ -124,12 +124,15 @@ __device__ __forceinline__ double rho_recip(E1DArgs const & a, int64_t it)
 __device__ __forceinline__ void cfl_at(E1DArgs const & a, int64_t it, double hdt, double r)
 {
     double const ga = a.gamma[it];
-    double m2 = a.so0[it * 3 + 1];
-    m2 *= m2;
+    double const m = a.so0[it * 3 + 1];
+    double const m2 = m * m;
     double const ke = 0.5 * m2 * r;
     double pr = (ga - 1.0) * (a.so0[it * 3 + 2] - ke);
     pr = (pr + fabs(pr)) / 2.0;
-    double const wspd = sqrt(ga * pr * r) + sqrt(m2) * r;
+    // The reference's sqrt(m * m) is |m| exactly: in binary IEEE arithmetic
+    // the square root of a correctly rounded square returns the operand's
+    // magnitude (barring overflow or underflow of the square).
+    double const wspd = sqrt(ga * pr * r) + fabs(m) * r;
     double const dxpos = a.coord[it + 1] - a.coord[it];
     double const dxneg = a.coord[it] - a.coord[it - 1];
     a.cfl[it] = hdt * wspd / (dxpos < dxneg ? dxpos : dxneg);

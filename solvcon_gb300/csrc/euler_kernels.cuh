@@ -273,27 +273,27 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     R const tau = a.taumin + acfl * a.tauscale;
     R const ofg1 = R(1) / R(NFGE);
 
-    // The gradient-element displacements P, Q, R of every face.
-    R gp[NFC][ND], gq[NFC][ND], gr[NFC][ND];
+    // Gradient-evaluation displacements: idis = dst - delta, dst = P + tau Q.
+    // With FP32 geometry P = mid - mean(mid) and Q = mean(dB) - dB are formed
+    // here from the face means (the faces' values are read again rather than
+    // held: they hit in L1, and registers bound this kernel's occupancy).
+    R mm[ND], mb[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        mm[d] = R(0);
+        mb[d] = R(0);
+    }
     if constexpr (D::MID)
     {
-        R mm[ND], mb[ND];
-#pragma unroll
-        for (int d = 0; d < ND; ++d)
-        {
-            mm[d] = R(0);
-            mb[d] = R(0);
-        }
 #pragma unroll
         for (int f = 0; f < NFC; ++f)
         {
 #pragma unroll
             for (int d = 0; d < ND; ++d)
             {
-                gp[f][d] = fg<ND>(a, f, D::K_MID + d, icl);
-                gr[f][d] = fg<ND>(a, f, D::K_DB + d, icl);
-                mm[d] += gp[f][d];
-                mb[d] += gr[f][d];
+                mm[d] += fg<ND>(a, f, D::K_MID + d, icl);
+                mb[d] += fg<ND>(a, f, D::K_DB + d, icl);
             }
         }
         R const inv = R(1) / R(NFC);
@@ -303,34 +303,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             mm[d] *= inv;
             mb[d] *= inv;
         }
-#pragma unroll
-        for (int f = 0; f < NFC; ++f)
-        {
-#pragma unroll
-            for (int d = 0; d < ND; ++d)
-            {
-                gq[f][d] = mb[d] - gr[f][d];
-                gp[f][d] -= mm[d];
-                gr[f][d] -= mm[d];
-            }
-        }
     }
-    else
-    {
-#pragma unroll
-        for (int f = 0; f < NFC; ++f)
-        {
-#pragma unroll
-            for (int d = 0; d < ND; ++d)
-            {
-                gp[f][d] = fg<ND>(a, f, D::K_P + d, icl);
-                gq[f][d] = fg<ND>(a, f, D::K_Q + d, icl);
-                gr[f][d] = fg<ND>(a, f, D::K_R + d, icl);
-            }
-        }
-    }
-
-    // Gradient-evaluation displacements: idis = dst - delta, dst = P + tau Q.
     R idis[NFC][ND];
 #pragma unroll
     for (int f = 0; f < NFC; ++f)
@@ -338,7 +311,15 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
-            idis[f][d] = gp[f][d] + tau * gq[f][d];
+            if constexpr (D::MID)
+            {
+                idis[f][d] = (fg<ND>(a, f, D::K_MID + d, icl) - mm[d]) +
+                             tau * (mb[d] - fg<ND>(a, f, D::K_DB + d, icl));
+            }
+            else
+            {
+                idis[f][d] = fg<ND>(a, f, D::K_P + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl);
+            }
         }
     }
     R delta[ND];
@@ -400,7 +381,15 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
-            jd[d] = gr[f][d] + tau * gq[f][d] - delta[d];
+            if constexpr (D::MID)
+            {
+                R const db = fg<ND>(a, f, D::K_DB + d, icl);
+                jd[d] = (db - mm[d]) + tau * (mb[d] - db) - delta[d];
+            }
+            else
+            {
+                jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+            }
         }
 #pragma unroll
         for (int i = 0; i < NEQ; ++i)
@@ -796,6 +785,17 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
 
 template <int ND, typename R, typename G, int CT1 = 0>
 __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
+{
+    fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+}
+
+// The same kernel asking the compiler for 5 resident blocks of 128 (at most
+// 102 registers): the 3D FP32 tetrahedron kernel, latency-bound at the 4
+// blocks its 106 registers allow, measured 4.7% faster so (more blocks
+// spill).  A stated minimum of 1 would instead free the compiler to use up
+// to 255 registers, so the other kernels keep the one-argument bound.
+template <int ND, typename R, typename G, int CT1>
+__global__ void __launch_bounds__(128, 5) k_fused_5(MarchArgs<R, G> a)
 {
     fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
