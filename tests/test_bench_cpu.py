@@ -1,0 +1,57 @@
+"""bench.py's host-side parts on the CPU: the oracle's all-core throughput
+run, the sizes of its samples, and the reference arm's JSON line for the
+multidim and the spacetime workloads (the GPU arm is exercised on the GPU)."""
+
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_cpu_sample_sizes():
+    sys.path.insert(0, ROOT)
+    import bench
+    for wl in ("tri2d", "tet3d", "tube1d", "spacetime"):
+        big, small = bench.cpu_nside(wl, 10), bench.cpu_nside(wl, 1000)
+        assert big >= small > 0
+    assert bench.cpu_nside("tube1d", 5) % 2 == 1
+
+
+def test_oracle_throughput_all_processes():
+    sys.path.insert(0, ROOT)
+    import bench
+    rate, units, nproc, secs = bench.oracle_throughput("tri2d", 8, 2,
+                                                       warmup=1, nproc=2)
+    assert nproc == 2 and units == 2 * 8 * 8 and rate > 0 and secs > 0
+
+
+def _reference_line(*extra):
+    run = subprocess.run([sys.executable, "bench.py", "--impl", "reference",
+                          "--steps", "3", "--warmup", "3"] + list(extra),
+                         cwd=ROOT, capture_output=True, text=True,
+                         timeout=600)
+    assert run.returncode == 0, run.stderr[-2000:]
+    lines = [json.loads(x) for x in run.stdout.splitlines()
+             if x.startswith("{")]
+    assert len(lines) == 1
+    return lines[0]
+
+
+def test_reference_arm_line_multidim():
+    line = _reference_line("--workload", "tri2d", "--cpu-nside", "10")
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup",
+                "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == "cell-steps/s"
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["value"] == line["value"]
+
+
+def test_reference_arm_line_spacetime():
+    line = _reference_line("--workload", "spacetime", "--cpu-nside", "500")
+    assert line["metric"] == "point-steps/s" and line["value"] > 0
+    assert line["config"]["sample_units"] == 2 * 500 + 1
