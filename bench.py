@@ -17,9 +17,12 @@ substep kernel (HBM bytes are the algorithmic bytes of one cell-substep); the
 FP64-pipe roofline beside it; ``cpu_baseline`` = the CPU oracle on a bounded
 sample; clocks sampled during the timed region.
 
-``--impl reference`` times the reference algorithm on the host CPU instead
-(the C oracle, a restatement of the reference march: the reference itself
-cannot be built on the GPU host, which has no copy of its sources).
+``--impl reference`` times the reference algorithm on the host CPU instead,
+one process per host core (the C oracle, a restatement of the reference
+march that equals the compiled reference bit for bit: the reference library
+is built from the reference's sources, which a machine without them cannot
+do).  The line then carries that rate in ``value``, ``cpu_baseline`` and
+``e2e``.
 Under torchrun with N > 1 every rank marches its own mesh (replicas: a single
 mesh is not decomposed), times are maxed over ranks and the value is the sum.
 """

@@ -9,7 +9,8 @@
  * reference lines it follows and keeps the reference's operation order, so
  * that on the same inputs it reproduces the reference's results to the last
  * bit or close to it.  Only tests/, the smoke check and bench.py's CPU
- * baseline use it, as the checker; the product never links it.
+ * baseline and reference arm use it, to check and to time against; the
+ * product never links it.
  *
  * All tables are whole buffers in the reference layout, ghost rows first.
  */

@@ -1,8 +1,9 @@
 """Python front of the C oracle (oracle/cese_oracle.c) -- TEST INFRASTRUCTURE.
 
 The oracle restates the reference CESE march on the CPU; tests,
-``__graft_entry__.smoke()`` and ``bench.py``'s CPU baseline use it as the
-checker.  The product never imports this module.
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU baseline and reference
+arm use it, to check results against and to time.  The product never imports
+this module.
 """
 
 import ctypes

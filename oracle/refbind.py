@@ -4,7 +4,8 @@ The library is the reference solvcon implementation itself (its own mesh,
 multidim and onedim sources, built by ``make -C oracle ref``) behind the thin C
 driver in oracle/ref_driver.cpp.  It is only present where the reference source
 tree was available at build time; :func:`available` says whether it is.  Only
-tests and the golden-vector generator use it, as a checker.
+tests and the golden-vector generator use it, to pin the oracle and the
+fixtures to the reference's own results.
 """
 
 import ctypes

@@ -2,8 +2,8 @@
 
 Compiles every translation unit under csrc/ with nvcc in parallel and links
 them into solvcon_gb300/_lib/libscg.so, in-tree.  Host C++ is compiled with
--ffp-contract=off so that the host mesh builder produces the same bits on the
-x86 build host and on the Arm GPU host.
+-ffp-contract=off so that the host mesh builder produces the same bits on
+x86-64 and on aarch64 hosts.
 """
 
 import concurrent.futures

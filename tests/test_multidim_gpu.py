@@ -3,8 +3,8 @@ with the oracle, per operation and over multi-step marches.
 
 Modelled on the reference's tests/test_multidim.py (solution storage, CFL,
 flux homogeneity, free stream, linear-field gradient recovery, boundary
-conditions, bounded channel march), with the CPU oracle (a bit-exact
-restatement of the reference, pinned in test_oracle.py) as the checker.
+conditions, bounded channel march), compared with the CPU oracle (a bit-exact
+restatement of the reference, pinned in test_oracle.py).
 
 Tolerances (FP64): one operation on the same inputs agrees with the oracle to
 1e-12 relative to the largest magnitude of the compared array (the GPU
