@@ -51,12 +51,14 @@ ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
              ("tet3d", "fp32-geom64"): 928, ("tet3d", "fp32"): 560}
 
 # DRAM bytes (read + write) and FP64 flops (DFMA counted as 2) of the fused
-# substep kernel per cell-substep, from one ncu capture each (profiles/
-# fused_substep_{tri2d_fp64,tri2d_fp32,tet3d_fp64}.md); absent until captured.  The FP64
-# records carry a primitive cache (192 B instead of 128 B), which trades
-# DRAM bytes, idle in the FP64-bound march, for FP64 operations.
+# substep kernel per cell-substep, each from one ncu capture of the kernel on
+# a smaller mesh of the same workload, larger than L2 (tri2d: 500^2 x 2 cells
+# FP64, 700^2 x 2 FP32; tet3d: 40^3 x 6 FP64, 60^3 x 6 FP32), divided by its
+# cells; absent until captured.  The FP64 records carry a primitive cache
+# (192 B instead of 128 B), which trades DRAM bytes, idle in the FP64-bound
+# march, for FP64 operations.
 NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 770.2, ("tri2d", "fp32"): 270.2,
-                        ("tet3d", "fp64"): 1337.3}
+                        ("tet3d", "fp64"): 1337.3, ("tet3d", "fp32"): 626.2}
 NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1195.6, ("tet3d", "fp64"): 2717.4}
 
 WORKLOADS = {
