@@ -321,11 +321,16 @@ del _n
 
 
 class GradientElement:
-    """Per-cell gradient element geometry (GradientElement.cpp:305-458).
+    """Per-cell gradient element geometry: solvcon's GradientElement
+    (cpp/solvcon/multidim/GradientElement.cpp:137-290, the sub-element table
+    at :16-79) with the bounds-checked accessors of its Python wrapper
+    (cpp/solvcon/multidim/pymod/wrap_multidim.cpp:42-204).
 
     Host-side helper with the reference's accessors (``rcl``, ``idis``,
     ``jdis``, ``faces``, ``displacement_matrix``, ``solve_gradient``); the
-    march itself evaluates the same geometry inside its kernels.
+    march itself evaluates the same geometry inside its kernels.  Face and
+    dimension indices out of range raise ``IndexError``; a ``udf`` whose
+    length is not ``ndim`` raises ``ValueError``.
     """
 
     _FGE = {
@@ -419,5 +424,18 @@ class GradientElement:
         if len(udf) != self.ndim:
             raise ValueError("GradientElement: udf size %d must equal ndim %d"
                              % (len(udf), self.ndim))
-        dst = np.array(self.displacement_matrix(ifge))
-        return np.linalg.solve(dst, np.asarray(udf, dtype="float64")).tolist()
+        # Cramer's rule with the inverse's columns written as cross products
+        # of the rows (3D) or the rotated rows (2D): grad = adj(dst) udf /
+        # det(dst), as the reference computes it, so a degenerate element
+        # gives inf/nan rather than an exception.
+        r = np.array(self.displacement_matrix(ifge), dtype="float64")
+        u = np.asarray(udf, dtype="float64")
+        if self.ndim == 2:
+            c = np.array([[r[1, 1], -r[0, 1]], [-r[1, 0], r[0, 0]]])
+            det = r[0, 0] * r[1, 1] - r[0, 1] * r[1, 0]
+        else:
+            c = np.stack([np.cross(r[1], r[2]), np.cross(r[2], r[0]),
+                          np.cross(r[0], r[1])], axis=1)
+            det = float(r[0] @ c[:, 0])
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return (c @ u / np.float64(det)).tolist()
