@@ -79,12 +79,12 @@ int scg_mesh_array(scg_mesh * mesh, int which, void ** data, int64_t * shape, in
                    int * dtype);
 /* build_interior(do_metric, do_edge): StaticMesh.hpp:363-374. */
 int scg_mesh_build_interior(scg_mesh * mesh, int do_metric, int do_edge);
-/* build_edge: StaticMesh_interior.cpp:545. */
+/* build_edge: StaticMesh_interior.cpp:566-621. */
 int scg_mesh_build_edge(scg_mesh * mesh);
 /* build_interior on the GPU: face extraction, de-duplication and numbering,
  * face-cell relations and metrics in device kernels, the tables copied back;
  * every table equals scg_mesh_build_interior's entry for entry
- * (StaticMesh_interior.cpp:332-977 restated per face and per cell).  Needs a
+ * (StaticMesh_interior.cpp:17-977 restated per face and per cell).  Needs a
  * GPU and a mesh without ghost layer whose cells all have the mesh's
  * dimension (others go to the host builder or give SCG_EINVAL). */
 int scg_mesh_build_interior_device(scg_mesh * mesh, int do_metric, int do_edge);
@@ -141,7 +141,7 @@ int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
 #define SCG_EA_CFLC 11
 #define SCG_EA_GAMMA 12
 
-/* EulerCore operation ids for scg_euler_op (wrap_multidim.cpp:269-319). */
+/* EulerCore operation ids for scg_euler_op (wrap_multidim.cpp:270-328). */
 #define SCG_OP_PREPARE_CE 0
 #define SCG_OP_UPDATE 1
 #define SCG_OP_CALC_SOLT 2
@@ -168,9 +168,9 @@ int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
  * it needs, so the mesh may be destroyed afterwards. */
 int scg_euler_create(const scg_mesh * mesh, double time_increment, int precision, scg_euler ** out);
 int scg_euler_destroy(scg_euler * core);
-/* out[5] = ndim ncell ngstcell neq precision (wrap_multidim.cpp:227-231). */
+/* out[5] = ndim ncell ngstcell neq precision (wrap_multidim.cpp:247-268). */
 int scg_euler_info(const scg_euler * core, int64_t * out);
-/* sigma0/taumin/tauscale properties and time_increment (wrap_multidim.cpp:311-316). */
+/* sigma0/taumin/tauscale properties and time_increment (wrap_multidim.cpp:313-316). */
 int scg_euler_get_param(const scg_euler * core, int which, double * value);
 int scg_euler_set_param(scg_euler * core, int which, double value);
 /* Shape (up to 3 extents) and ghost count of an array in the reference layout. */
@@ -179,7 +179,7 @@ int scg_euler_array_shape(const scg_euler * core, int which, int64_t * shape, in
  * count is the number of float64 elements in the host buffer. */
 int scg_euler_get(scg_euler * core, int which, double * host, int64_t count);
 int scg_euler_set(scg_euler * core, int which, const double * host, int64_t count);
-/* init_solution(gamma, rho, v, p): euler_solution.cpp:188-233. */
+/* init_solution(gamma, rho, v, p): euler_solution.cpp:54-99. */
 int scg_euler_init_solution(scg_euler * core, double gamma, double rho, const double * v, int nv, double p);
 /* add_nonrefl/add_slipwall/add_inlet: euler_bc.cpp:324-391. */
 int scg_euler_add_bc(scg_euler * core, int kind, const int32_t * faces, int64_t nface, const double * value,

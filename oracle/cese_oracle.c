@@ -530,7 +530,7 @@ void ora_bc_dsoln(ora_euler * e)
     }
 }
 
-/* ---- calc_cfl (euler_solution.cpp:240-294) ------------------------------ */
+/* ---- calc_cfl (euler_solution.cpp:106-160) ------------------------------ */
 
 void ora_calc_cfl(ora_euler * e)
 {
@@ -574,7 +574,7 @@ void ora_calc_cfl(ora_euler * e)
     }
 }
 
-/* ---- GradientElement (GradientElement.cpp:16-458) ----------------------- */
+/* ---- GradientElement (GradientElement.cpp:16-290) ----------------------- */
 
 typedef struct
 {
@@ -650,7 +650,7 @@ static void gelem_build(const ora_euler * e, int64_t icl, double tau, gelem_t * 
             avg[d] += gp[ifl][d];
     for (int d = 0; d < nd; ++d)
         avg[d] /= g->clnfc;
-    /* calc_gge_centroid (GradientElement.cpp:249-301). */
+    /* calc_gge_centroid (GradientElement.cpp:81-133). */
     double cnd[3] = {0, 0, 0};
     double voc = 0.0;
     for (int isub = 0; isub < g->ge.nfge; ++isub)

@@ -224,7 +224,7 @@ __global__ void k_bc1(MarchArgs<R, G> a, int32_t const * gint)
     }
 }
 
-// init_solution (euler_solution.cpp:188-233): so0n body rows and every gamma.
+// init_solution (euler_solution.cpp:54-99): so0n body rows and every gamma.
 template <int ND, typename R>
 __global__ void k_init(R * nxt, R * gamma, int64_t ngst, int64_t nrow, double ga, double rho, double m0, double m1,
                        double m2, double energy)

@@ -17,13 +17,13 @@
  *    sub-face centroids and normals, so each face's sub-faces are folded into
  *    two geometric moments at set-up: N = sum_sf n_sf and
  *    M[e][d] = sum_sf (x_sf - x_j)[e] n_sf[d] (pre-scaled by dt/2).
- *  - The gradient element (GradientElement.cpp:305-381) is linear in tau, so
+ *  - The gradient element (GradientElement.cpp:137-213) is linear in tau, so
  *    its displacement vectors are idis = P + tau Q - delta and
  *    jdis = R + tau Q - delta with P, Q, R precomputed per face; for simplices
  *    the sub-element centroid shift delta is exactly zero (the fan of a
  *    simplex about its vertex mean has equal sub-volumes).
  *  - Each fundamental gradient element's 2x2/3x3 solve
- *    (GradientElement.cpp:447-458) uses its inverse's rows once per cell,
+ *    (GradientElement.cpp:215-290) uses its inverse's rows once per cell,
  *    instead of an adjugate and determinant per equation.
  *
  * Results equal the reference's up to floating-point round-off.
@@ -95,7 +95,7 @@ struct Rec
 };
 
 // Small constants of the reference, with FP32-safe floors.  The FP64 values
-// are the reference's own (euler_march.cpp:30, euler_solution.cpp:242,
+// are the reference's own (euler_march.cpp:30, euler_solution.cpp:108,
 // euler_gradient.cpp:28); 1e-60 and 1e-200 underflow in FP32, so the FP32
 // march uses the smallest floors that keep the same expressions finite.
 template <typename R>

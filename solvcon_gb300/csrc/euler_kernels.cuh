@@ -214,7 +214,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
     }
 }
 
-// calc_cfl for one body cell (euler_solution.cpp:240-294): original and
+// calc_cfl for one body cell (euler_solution.cpp:106-160): original and
 // clamped CFL, and the energy rewritten from the non-negative pressure.  The
 // reference's three divisions by rho use one reciprocal 1/(rho + TINY) (the
 // floor changes nothing unless rho is below 1e-44 in FP64, 1e-23 in FP32,
@@ -253,7 +253,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 }
 
 // calc_dsoln for one body cell (euler_gradient.cpp:23-130 with the gradient
-// element of GradientElement.cpp:305-458): per fundamental gradient element
+// element of GradientElement.cpp:137-290): per fundamental gradient element
 // solve, W-1/2 weights, W-3/4 cap, weighted sum.  The neighbour records are
 // gathered a second time (calc_soln just read them, so the loads hit in
 // cache); carrying calc_soln's neighbour terms over instead costs more FP64
@@ -331,7 +331,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     if constexpr (!CellT<CT>::SIMPLEX)
     {
         // Sub-element centroid of the gradient element about the vertex mean
-        // (calc_gge_centroid, GradientElement.cpp:249-301).
+        // (calc_gge_centroid, GradientElement.cpp:81-133).
         R voc = R(0);
 #pragma unroll
         for (int k = 0; k < NFGE; ++k)

@@ -4,7 +4,7 @@
  * The faces of each cell type: for every face its type, its node count and
  * the positions of its nodes in the cell's node list, in the order the
  * reference's FaceBuilder emits them (cpp/solvcon/mesh/StaticMesh_interior.cpp
- * :26-330).  The order of the faces and of their nodes decides the face
+ * :26-310).  The order of the faces and of their nodes decides the face
  * numbering and the face orientation of a built mesh, so both mesh builders
  * (host and device) read this one table.
  */

@@ -1,7 +1,7 @@
 /*
  * StaticMesh::build_interior on the GPU: the faces of every cell, their
  * de-duplication and numbering, the face-cell relations and the metrics
- * (cpp/solvcon/mesh/StaticMesh_interior.cpp:332-977), giving tables equal to
+ * (cpp/solvcon/mesh/StaticMesh_interior.cpp:17-977), giving tables equal to
  * the host builder's (mesh_host.cpp) entry for entry.
  *
  *  1. Every cell writes its faces into consecutive slots (slot order = cell

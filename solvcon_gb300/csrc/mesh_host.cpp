@@ -146,7 +146,7 @@ void HostMesh::build_faces_from_cells()
         }
     }
 
-    // make_ndfcs (StaticMesh_interior.cpp:386-421): faces touching each node,
+    // make_ndfcs (StaticMesh_interior.cpp:388-426): faces touching each node,
     // in ascending face order.
     std::vector<int64_t> ndoff(static_cast<size_t>(nnode) + 1, 0);
     for (int64_t ifc = 0; ifc < mface; ++ifc)
@@ -171,7 +171,7 @@ void HostMesh::build_faces_from_cells()
         }
     }
 
-    // make_dedupmap (StaticMesh_interior.cpp:426-477).
+    // make_dedupmap (StaticMesh_interior.cpp:428-477).
     std::vector<int64_t> dedup(static_cast<size_t>(mface));
     std::iota(dedup.begin(), dedup.end(), 0);
     auto count_match = [&](int64_t ifc, int64_t jfc)
@@ -298,7 +298,7 @@ void HostMesh::build_edge()
 
 // Face centroids, unit normals and areas, cell centroids and volumes, with
 // face re-orientation so that each face normal points out of fccls[0]
-// (StaticMesh_interior.cpp:600-977).
+// (StaticMesh_interior.cpp:623-977).
 void HostMesh::calc_metric()
 {
     if (ndim == 2)
@@ -405,7 +405,7 @@ void HostMesh::calc_metric()
     }
 
     // Cell centroids: node average, then the face-pyramid weighted centroid
-    // (StaticMesh_interior.cpp:754-919; in-centres are off by default).
+    // (StaticMesh_interior.cpp:770-925; in-centres are off by default).
     double const frac = (ndim == 2) ? 3.0 : 4.0;
     for (int64_t icl = 0; icl < ncell; ++icl)
     {
@@ -449,7 +449,7 @@ void HostMesh::calc_metric()
         }
     }
 
-    // Volumes with face re-orientation (StaticMesh_interior.cpp:922-977).
+    // Volumes with face re-orientation (StaticMesh_interior.cpp:926-977).
     auto reorder_face = [this](int32_t ifc)
     {
         int const nnd = fcnds(ifc, 0);

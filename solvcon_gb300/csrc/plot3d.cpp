@@ -27,7 +27,7 @@ namespace
 
 // Grid offsets (di, dj, dk) of the hexahedron's corners from cell (i, j, k),
 // in solvcon's corner order: the x = i - 1 face then the x = i face, each
-// around (j, k) (plot3d.cpp:96-104).  The order defines the cells read.
+// around (j, k) (plot3d.cpp:88-96).  The order defines the cells read.
 constexpr int HEX_CORNER[8][3] = {{-1, -1, -1}, {-1, 0, -1}, {-1, 0, 0}, {-1, -1, 0},
                                   {0, -1, -1},  {0, 0, -1},  {0, 0, 0},  {0, -1, 0}};
 

@@ -48,7 +48,7 @@ def _flux(u, gamma):
     return f
 
 
-# -- solution storage and initialisation (test_multidim.py:394-600) ---------
+# -- solution storage and initialisation (test_multidim.py:450-599) ---------
 
 @pytest.mark.parametrize("name", sorted(FIXTURES))
 def test_storage_and_init(name):
@@ -123,7 +123,7 @@ def test_update_swaps_buffers():
     np.testing.assert_array_equal(view, ec.so1c.ndarray)
 
 
-# -- marching primitives (test_multidim.py:632-770) -------------------------
+# -- marching primitives (test_multidim.py:600-789) -------------------------
 
 @pytest.mark.parametrize("name", sorted(FIXTURES))
 def test_calc_solt_is_minus_flux_combination(name):
