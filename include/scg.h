@@ -353,7 +353,10 @@ int scg_st_stream(const scg_st * solver, void ** out);
 /* Device FMA throughput in TFLOP/s for SCG_FP64 or SCG_FP32 (a register-only
  * FMA chain over all SMs, iters FMAs-per-accumulator). */
 int scg_fma_peak(int precision, int iters, double * tflops);
-/* Page-locked host buffers for end-to-end host<->device copies. */
+/* Page-locked host blocks, mapped into the device's address space.  A table
+ * that lies inside such a block moves through scg_euler_get / scg_euler_set
+ * with one gather or scatter kernel over the host link and no staging copy;
+ * any other host pointer goes through a device staging table. */
 int scg_host_alloc(int64_t nbytes, void ** out);
 int scg_host_free(void * ptr);
 /* CUDA events (cudaEvent_t) recorded on a stream, and their elapsed time. */

@@ -38,6 +38,12 @@ std::string const & last_error();
 // Count of kernels this library has launched (for the bench's gpu_launches).
 extern std::atomic<int64_t> g_launches;
 
+// The device address of the host range [p, p + nbytes) when the whole range
+// lies inside one block from scg_host_alloc (page-locked and mapped into the
+// device's address space), else nullptr.  Kernels may then load and store
+// the range directly over the host link, with no staging copy.
+void * mapped_host(void const * p, size_t nbytes);
+
 inline void cuda_check(cudaError_t rc, char const * what)
 {
     if (rc != cudaSuccess)

@@ -279,6 +279,72 @@ __global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, i
     }
 }
 
+// The same record fields read from or written to mapped host memory: one
+// thread per pair of consecutive doubles of the host table, so the host side
+// is accessed in contiguous 16-byte pieces (vec: the host table is 16-byte
+// aligned) and the records are gathered on the device.
+template <int ND, typename R>
+__global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int off, int width, bool vec)
+{
+    int64_t const n = nrow * width;
+    int64_t const i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    if (i >= n)
+    {
+        return;
+    }
+    int64_t const r0 = i / width;
+    int const k0 = static_cast<int>(i - r0 * width);
+    double const v0 = double(rec[r0 * Rec<ND, R>::RS + off + k0]);
+    if (i + 1 >= n)
+    {
+        out[i] = v0;
+        return;
+    }
+    int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
+    int const k1 = k0 + 1 < width ? k0 + 1 : 0;
+    double const v1 = double(rec[r1 * Rec<ND, R>::RS + off + k1]);
+    if (vec)
+    {
+        *reinterpret_cast<double2 *>(out + i) = make_double2(v0, v1);
+    }
+    else
+    {
+        out[i] = v0;
+        out[i + 1] = v1;
+    }
+}
+
+template <int ND, typename R>
+__global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int off, int width, bool vec)
+{
+    int64_t const n = nrow * width;
+    int64_t const i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    if (i >= n)
+    {
+        return;
+    }
+    int64_t const r0 = i / width;
+    int const k0 = static_cast<int>(i - r0 * width);
+    if (i + 1 >= n)
+    {
+        rec[r0 * Rec<ND, R>::RS + off + k0] = R(in[i]);
+        return;
+    }
+    double2 v;
+    if (vec)
+    {
+        v = *reinterpret_cast<double2 const *>(in + i);
+    }
+    else
+    {
+        v = make_double2(in[i], in[i + 1]);
+    }
+    int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
+    int const k1 = k0 + 1 < width ? k0 + 1 : 0;
+    rec[r0 * Rec<ND, R>::RS + off + k0] = R(v.x);
+    rec[r1 * Rec<ND, R>::RS + off + k1] = R(v.y);
+}
+
 template <typename R>
 __global__ void k_to_f64(R const * in, double * out, int64_t n)
 {
@@ -918,6 +984,15 @@ public:
             R * base;
             int off, width;
             field_of(which, base, off, width);
+            if (double * const dev = static_cast<double *>(mapped_host(out, nb)))
+            {
+                // Mapped host table: the gather writes it directly.
+                k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
+                    base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                launched(stream, "get_field_host");
+                sync();
+                return;
+            }
             k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width);
             launched(stream, "get_field");
         }
@@ -938,8 +1013,24 @@ public:
         {
             return;
         }
-        double * const tmp = staging(n);
         size_t const nb = static_cast<size_t>(n) * sizeof(double);
+        if (which >= EA_SO0C && which <= EA_SO1N)
+        {
+            if (double const * const dev = static_cast<double const *>(mapped_host(in, nb)))
+            {
+                // Mapped host table: the scatter reads it directly.
+                R * base;
+                int off, width;
+                field_of(which, base, off, width);
+                k_set_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
+                    base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                launched(stream, "set_field_host");
+                next_valid = false;
+                sync();
+                return;
+            }
+        }
+        double * const tmp = staging(n);
         cuda_check(cudaMemcpyAsync(tmp, in, nb, cudaMemcpyHostToDevice, stream), "H2D");
         if (which >= EA_CEVOL && which <= EA_SFNML)
         {

@@ -8,7 +8,43 @@
 #include "../../include/scg.h"
 #include "common.hpp"
 
+#include <cstdint>
+#include <map>
+#include <mutex>
 #include <vector>
+
+namespace
+{
+
+// Blocks from scg_host_alloc: host address -> (bytes, device address).
+struct HostBlock
+{
+    size_t nbytes;
+    void * dev;
+};
+std::mutex g_blocks_mutex;
+std::map<uintptr_t, HostBlock> g_blocks;
+
+} // namespace
+
+void * scg::mapped_host(void const * p, size_t nbytes)
+{
+    uintptr_t const a = reinterpret_cast<uintptr_t>(p);
+    std::lock_guard<std::mutex> lk(g_blocks_mutex);
+    auto it = g_blocks.upper_bound(a);
+    if (it == g_blocks.begin())
+    {
+        return nullptr;
+    }
+    --it;
+    HostBlock const & b = it->second;
+    uintptr_t const off = a - it->first;
+    if (!b.dev || off > b.nbytes || nbytes > b.nbytes - off)
+    {
+        return nullptr;
+    }
+    return static_cast<char *>(b.dev) + off;
+}
 
 namespace
 {
@@ -89,12 +125,27 @@ int scg_fma_peak(int precision, int iters, double * tflops)
 int scg_host_alloc(int64_t nbytes, void ** out)
 {
     return scg::guarded([&] {
+        if (nbytes < 0 || !out)
+        {
+            throw std::invalid_argument("scg_host_alloc: negative size or null out");
+        }
         void * p = nullptr;
-        cudaError_t rc = cudaHostAlloc(&p, static_cast<size_t>(nbytes), cudaHostAllocDefault);
+        cudaError_t rc = cudaHostAlloc(&p, static_cast<size_t>(nbytes), cudaHostAllocMapped);
         if (rc != cudaSuccess)
         {
             (void)cudaGetLastError();
             throw std::bad_alloc();
+        }
+        void * d = nullptr;
+        rc = cudaHostGetDevicePointer(&d, p, 0);
+        if (rc != cudaSuccess)
+        {
+            (void)cudaGetLastError();
+            d = nullptr;
+        }
+        {
+            std::lock_guard<std::mutex> lk(g_blocks_mutex);
+            g_blocks[reinterpret_cast<uintptr_t>(p)] = {static_cast<size_t>(nbytes), d};
         }
         *out = p;
     });
@@ -102,7 +153,13 @@ int scg_host_alloc(int64_t nbytes, void ** out)
 
 int scg_host_free(void * p)
 {
-    return scg::guarded([&] { scg::cuda_check(cudaFreeHost(p), "cudaFreeHost"); });
+    return scg::guarded([&] {
+        {
+            std::lock_guard<std::mutex> lk(g_blocks_mutex);
+            g_blocks.erase(reinterpret_cast<uintptr_t>(p));
+        }
+        scg::cuda_check(cudaFreeHost(p), "cudaFreeHost");
+    });
 }
 
 int scg_event_create(void ** out)

@@ -1,0 +1,125 @@
+"""Solution tables exchanged through page-locked, mapped host blocks.
+
+``scg_euler_get`` / ``scg_euler_set`` on a host table that lies inside a
+block from ``scg_host_alloc`` skip the device staging copy: one kernel
+gathers the records straight into the host table (or scatters the host
+table into the records) over the host link.  Every other host pointer goes
+through the staging copy.  Both routes must give the same tables, bit for
+bit, and a march continued after either route must give the same state.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RECORD_TABLES = {"so0c": 4, "so0n": 5, "so0t": 6, "so1c": 7, "so1n": 8}
+
+
+class _Block:
+    """A scg_host_alloc block with a float64 view starting ``skip`` values
+    into it (skip = 1 gives a table that is 8- but not 16-byte aligned)."""
+
+    def __init__(self, nvalue, skip=0):
+        from solvcon_gb300._lib import check, lib
+        self._lib = lib
+        self.ptr = ctypes.c_void_p()
+        check(lib.scg_host_alloc(8 * (nvalue + skip), ctypes.byref(self.ptr)))
+        raw = (ctypes.c_double * (nvalue + skip)).from_address(self.ptr.value)
+        self.view = np.ctypeslib.as_array(raw)[skip:]
+        self.addr = self.ptr.value + 8 * skip
+
+    def free(self):
+        from solvcon_gb300._lib import check
+        check(self._lib.scg_host_free(self.ptr))
+
+
+def _marched_core(precision, ndim):
+    import solvcon_gb300 as sg
+    from solvcon_gb300 import meshgen
+    if ndim == 2:
+        x, t, c = meshgen.tri_square(24, 0.2, 3)
+    else:
+        x, t, c = meshgen.tet_cube(6, 0.15, 3)
+    mesh = meshgen.build_mesh(ndim, x, t, c)
+    ec = sg.EulerCore(mesh=mesh, time_increment=2e-3, precision=precision)
+    clcnd = np.array(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    state = (meshgen.quadrant_state(clcnd, seed=5) if ndim == 2
+             else meshgen.blast_state(clcnd))
+    ec.add_slipwall([int(f) for f in mesh.bndfcs.ndarray[:, 0]])
+    meshgen.set_state(ec, mesh, state, 1.4)
+    ec.march(3)
+    # From here on the tables move only through the C ABI calls below.
+    ec.release_views()
+    return ec
+
+
+def _get(core, which, shape):
+    """A table through the staging route (a pageable numpy table)."""
+    from solvcon_gb300._lib import check, lib, ptr
+    out = np.empty(shape, dtype="float64")
+    check(lib.scg_euler_get(core.handle, which, ptr(out), out.size))
+    return out
+
+
+def _shape(core, name):
+    total = core.ncell + core.ngstcell
+    if name.startswith("so1"):
+        return (total, core.neq, core.ndim)
+    if name.startswith("so0"):
+        return (total, core.neq)
+    return (total,)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("ndim", [2, 3])
+@pytest.mark.parametrize("skip", [0, 1])
+def test_get_through_mapped_block_equals_staged(precision, ndim, skip):
+    from solvcon_gb300._lib import check, lib
+    ec = _marched_core(precision, ndim)
+    for name, which in RECORD_TABLES.items():
+        staged = _get(ec, which, _shape(ec, name))
+        blk = _Block(staged.size, skip)
+        try:
+            blk.view[...] = np.nan
+            check(lib.scg_euler_get(ec.handle, which, ctypes.c_void_p(blk.addr),
+                                    staged.size))
+            np.testing.assert_array_equal(blk.view.reshape(staged.shape),
+                                          staged, err_msg=name)
+        finally:
+            blk.free()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("ndim", [2, 3])
+@pytest.mark.parametrize("skip", [0, 1])
+def test_set_through_mapped_block_equals_staged(precision, ndim, skip):
+    from solvcon_gb300._lib import check, lib, ptr
+    a = _marched_core(precision, ndim)
+    b = _marched_core(precision, ndim)
+    rng = np.random.default_rng(11)
+    for name in ("so0n", "so1n"):
+        which = RECORD_TABLES[name]
+        cur = _get(a, which, _shape(a, name))
+        new = cur * (1.0 + 1e-3 * rng.standard_normal(cur.shape))
+        # a: staging route (a pageable numpy table).
+        check(lib.scg_euler_set(a.handle, which, ptr(new), new.size))
+        # b: mapped route.
+        blk = _Block(new.size, skip)
+        try:
+            blk.view[...] = new.ravel()
+            check(lib.scg_euler_set(b.handle, which, ctypes.c_void_p(blk.addr),
+                                    new.size))
+        finally:
+            blk.free()
+        np.testing.assert_array_equal(_get(b, which, new.shape),
+                                      _get(a, which, new.shape), err_msg=name)
+    a.march(2)
+    b.march(2)
+    for name in ("so0n", "so1n", "cflo"):
+        which = {"so0n": 5, "so1n": 8, "cflo": 10}[name]
+        shape = _shape(a, name)
+        np.testing.assert_array_equal(_get(b, which, shape),
+                                      _get(a, which, shape), err_msg=name)
