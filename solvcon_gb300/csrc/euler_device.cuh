@@ -289,7 +289,7 @@ __device__ __forceinline__ void solt_row(R const * u, R const * g, R ga, R * t)
 }
 
 // Fundamental gradient element tables (1-based in GradientElement.cpp:
-// 184-247, 0-based here), per cell type.
+// 16-79, 0-based here), per cell type.
 template <int CT>
 struct CellT;
 

@@ -239,7 +239,10 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     R const pra = (pr + fabs(pr)) / R(2);
     R const wspd = sqr_t(ga * pra * ri) + sqr_t(momsq) * ri;
     R const cflo = wspd * R(ldg(a.cgeo + 1 * a.ncell + icl));
-    R const cflc = (cflo - R(1)) * pra / (pra + Tiny<R>::CFL) + R(1);
+    // pra / (pra + TINY) is exactly 1 whenever TINY does not change pra (any
+    // pressure above ~1e-44 in FP64), so the division is taken only below.
+    R const prt = pra + Tiny<R>::CFL;
+    R const cflc = (cflo - R(1)) * (prt == pra ? R(1) : pra / prt) + R(1);
     a.cflo[row] = cflo;
     a.cflc[row] = cflc;
     // The reference stores pra/ga1 + ke + TINY.  For pr > 0 that is exactly
@@ -269,7 +272,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     using D = Geo<ND, G>;
 
     R const acfl = fabs(cflc);
-    R const sgm0 = a.sigma0 / acfl;
+    R const sgm0 = sizeof(R) == 8 ? R(0) : a.sigma0 / acfl; // FP32 cap only
     R const tau = a.taumin + acfl * a.tauscale;
     R const ofg1 = R(1) / R(NFGE);
 
@@ -512,40 +515,90 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             wgt[k] = rsq(sq + Tiny<R>::AZ);
             wacc += wgt[k];
         }
-        R const rw = R(1) / wacc;
-        R wmax = R(0);
-        R wmin = R(0);
-#pragma unroll
-        for (int k = 0; k < NFGE; ++k)
+        if constexpr (sizeof(R) == 8)
         {
-            wgt[k] = wgt[k] * rw - ofg1;
-            wmax = fmax(wmax, wgt[k]);
-            wmin = fmin(wmin, wgt[k]);
-        }
-        // W-3/4 cap: sm = min(A / a1, B / a2) with A = 1 - 1/n > 0,
-        // a1 = wmax + TINY > 0, B = -1/n < 0, a2 = wmin - TINY < 0.  Both
-        // quotients are positive, and A / a1 <= B / a2 exactly when
-        // A a2 >= B a1, so the smaller one is chosen first and one division
-        // is taken instead of two.
-        R const a1 = wmax + Tiny<R>::AZ;
-        R const a2 = wmin - Tiny<R>::AZ;
-        bool const first = (R(1) - ofg1) * a2 >= -ofg1 * a1;
-        R const sm = (first ? R(1) - ofg1 : -ofg1) / (first ? a1 : a2);
-        R const sig = fmin(sm, sgm0);
-        if (sm < sgm0)
-        {
-            fired |= static_cast<uint8_t>(1u << i);
-        }
-#pragma unroll
-        for (int d = 0; d < ND; ++d)
-        {
-            R s = R(0);
+            // FP64: one division per equation.  With u = w - wacc/n (the
+            // deviations scaled by wacc > 0) the reference's weight
+            // 1/n + sm (w/wacc - 1/n) is 1/n + (sm/wacc) u, and each of its
+            // three caps divided by wacc is a quotient of known sign:
+            //   T1 = (1 - 1/n) / (umax + TINY wacc),  T2 = (1/n) / (TINY wacc - umin),
+            //   T0 = sigma0 / (|cfl| wacc).
+            // The smaller of T1, T2 is chosen by cross-multiplying as in
+            // FP32 below; it fires (the W-3/4 cap binds) when it is below
+            // T0, again by cross-multiplying, and only the chosen quotient
+            // is divided out.
+            R const wq = ofg1 * wacc;
+            R umax = R(0);
+            R umin = R(0);
 #pragma unroll
             for (int k = 0; k < NFGE; ++k)
             {
-                s += (ofg1 + sig * wgt[k]) * grad[k][d];
+                wgt[k] -= wq;
+                umax = fmax(umax, wgt[k]);
+                umin = fmin(umin, wgt[k]);
             }
-            so1n[i * ND + d] = s;
+            R const za = Tiny<R>::AZ * wacc;
+            R const d1 = umax + za;
+            R const d2 = za - umin;
+            bool const first = (R(1) - ofg1) * d2 <= ofg1 * d1;
+            R const nn = first ? R(1) - ofg1 : ofg1;
+            R const dd = first ? d1 : d2;
+            R const cw = acfl * wacc;
+            bool const fire = nn * cw < a.sigma0 * dd;
+            R const c = (fire ? nn : a.sigma0) / (fire ? dd : cw);
+            if (fire)
+            {
+                fired |= static_cast<uint8_t>(1u << i);
+            }
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                R s = R(0);
+#pragma unroll
+                for (int k = 0; k < NFGE; ++k)
+                {
+                    s += (ofg1 + c * wgt[k]) * grad[k][d];
+                }
+                so1n[i * ND + d] = s;
+            }
+        }
+        else
+        {
+            R const rw = R(1) / wacc;
+            R wmax = R(0);
+            R wmin = R(0);
+#pragma unroll
+            for (int k = 0; k < NFGE; ++k)
+            {
+                wgt[k] = wgt[k] * rw - ofg1;
+                wmax = fmax(wmax, wgt[k]);
+                wmin = fmin(wmin, wgt[k]);
+            }
+            // W-3/4 cap: sm = min(A / a1, B / a2) with A = 1 - 1/n > 0,
+            // a1 = wmax + TINY > 0, B = -1/n < 0, a2 = wmin - TINY < 0.  Both
+            // quotients are positive, and A / a1 <= B / a2 exactly when
+            // A a2 >= B a1, so the smaller one is chosen first and one
+            // division is taken instead of two.
+            R const a1 = wmax + Tiny<R>::AZ;
+            R const a2 = wmin - Tiny<R>::AZ;
+            bool const first = (R(1) - ofg1) * a2 >= -ofg1 * a1;
+            R const sm = (first ? R(1) - ofg1 : -ofg1) / (first ? a1 : a2);
+            R const sig = fmin(sm, sgm0);
+            if (sm < sgm0)
+            {
+                fired |= static_cast<uint8_t>(1u << i);
+            }
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                R s = R(0);
+#pragma unroll
+                for (int k = 0; k < NFGE; ++k)
+                {
+                    s += (ofg1 + sig * wgt[k]) * grad[k][d];
+                }
+                so1n[i * ND + d] = s;
+            }
         }
     }
     if (a.limiter)

@@ -84,7 +84,7 @@ void HostMesh::build_interior(bool do_metric, bool do_edge)
 }
 
 // Face extraction and de-duplication (FaceBuilder, StaticMesh_interior.cpp:
-// 331-528): populate every cell's faces, find duplicates through a
+// 17-543): populate every cell's faces, find duplicates through a
 // node-to-face table keyed on each face's first node, compact, and record the
 // two cells of each face in ascending cell order.
 void HostMesh::validate_cells() const
@@ -265,7 +265,7 @@ void HostMesh::build_faces_from_cells()
 }
 
 // Unique edges in first-seen order, lower node first (StaticMesh_interior.cpp:
-// 545-587).
+// 566-621).
 void HostMesh::build_edge()
 {
     std::set<std::pair<int32_t, int32_t>> known;
