@@ -57,9 +57,9 @@ ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
 # cells; absent until captured.  The FP64 records carry a primitive cache
 # (192 B instead of 128 B), which trades DRAM bytes, idle in the FP64-bound
 # march, for FP64 operations.
-NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 770.2, ("tri2d", "fp32"): 270.2,
+NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 769.5, ("tri2d", "fp32"): 270.2,
                         ("tet3d", "fp64"): 1337.3, ("tet3d", "fp32"): 626.2}
-NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1195.6, ("tet3d", "fp64"): 2717.4}
+NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1159.6, ("tet3d", "fp64"): 2717.4}
 
 WORKLOADS = {
     "tri2d": dict(ndim=2, nside=1000, jitter=0.2, cfl=0.8, seed=2026),
