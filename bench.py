@@ -796,15 +796,29 @@ def run_accuracy(args, world, rank, dist):
       CFL 0.8, 500 steps) against the CPU oracle itself.
 
     The FP64 GPU march is the reference at full size (the CPU oracle would
-    take hours); parity tests pin it to the oracle on smaller meshes."""
+    take hours); parity tests pin it to the oracle on smaller meshes.
+    ``--cases`` picks a subset (blast3d, batch, oracle2d; default all)."""
     from oracle import oracle as ora
-    from solvcon_gb300.batch import EulerBatch
     if rank != 0:
         return
     out = {"metric": "accuracy", "data": "synthetic"}
     rng = np.random.default_rng(1)
+    cases = set((args.cases or "blast3d,batch,oracle2d").split(","))
+    unknown = cases - {"blast3d", "batch", "oracle2d"}
+    if unknown:
+        raise SystemExit("--cases: unknown %s" % sorted(unknown))
+    if "blast3d" in cases:
+        _accuracy_blast3d(args, out, rng)
+    if "batch" in cases:
+        _accuracy_batch(args, out, rng)
+    if "oracle2d" in cases:
+        _accuracy_oracle2d(args, out, rng, ora)
+    print(json.dumps(out), flush=True)
 
-    # 3D blast.
+
+def _accuracy_blast3d(args, out, rng):
+    """The 3D spherical blast at full size: FP32 and perturbed FP64 against
+    FP64."""
     nside = args.nside or 160
     t0 = time.perf_counter()
     w, mesh, state, faces = make_workload("tet3d", nside=nside)
@@ -834,7 +848,11 @@ def run_accuracy(args, world, rank, dist):
     out["blast3d"] = res
     del finals
 
-    # Batched distribution, 1000 steps.
+
+def _accuracy_batch(args, out, rng):
+    """The batched distribution, 1000 steps: FP32 (batched) and perturbed
+    FP64 against FP64."""
+    from solvcon_gb300.batch import EulerBatch
     nmesh = args.nmesh
     data = batch_meshes(nmesh)
     dts = [dt_for_cfl_g(m, s, 0.8, g) for m, s, f, g in data]
@@ -877,7 +895,9 @@ def run_accuracy(args, world, rank, dist):
     out["batch"] = res
     del finals
 
-    # 2D sample against the CPU oracle.
+
+def _accuracy_oracle2d(args, out, rng, ora):
+    """A sample of the 2D four-quadrant workload against the CPU oracle."""
     steps = 500
     w, mesh, state, faces = make_workload("tri2d", nside=300)
     dt = dt_for_cfl(mesh, state, faces, 0.8)
@@ -906,8 +926,6 @@ def run_accuracy(args, world, rank, dist):
         res[name + "_vs_oracle"] = {"rel_l1": l1, "rel_linf": linf}
         del c
     out["quadrant2d_vs_oracle"] = res
-    print(json.dumps(out), flush=True)
-
 
 def run_meshbuild(args, world, rank, dist):
     """Time to first step of the 3D workload's mesh (160^3 x 6 tetrahedra by
@@ -985,6 +1003,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cases", default=None,
+                    help="accuracy workload: comma-separated subset of "
+                    "blast3d, batch, oracle2d")
     ap.add_argument("--nmesh", type=int, default=None)
     ap.add_argument("--nreq", type=int, default=64)
     ap.add_argument("--rates", default="50,200,1000,2000")

@@ -1221,7 +1221,7 @@ public:
         {
             if constexpr (ND == 3 && sizeof(R) == 4)
             {
-                k_fused_5<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+                k_fused_4<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
             }
             else
             {

@@ -123,6 +123,61 @@ __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t
     return R(ldg(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
 }
 
+// What calc_soln hands to calc_dsoln of the same cell when the neighbour
+// records are not gathered twice (FP32 tetrahedra, whose four 128-byte
+// neighbour records cost more to gather again than 40 registers cost to
+// keep; in 2D the extra registers lose more occupancy than the second
+// gather costs, measured 4% slower): the solution change at
+// face f's gradient-evaluation point is linear in tau,
+//   u_j + hdt ut_j + jdis . g_j - u_i  with  jdis = A_f + tau B_f,
+// so calc_soln, holding neighbour j's record, keeps
+//   p[f] = u_j + hdt ut_j + A_f . g_j  and  q[f] = B_f . g_j
+// per equation.  A_f = dB_f - mean(mid), B_f = mean(dB) - dB_f with FP32
+// geometry (R_f and Q_f with FP64 geometry); delta is zero for simplices.
+template <int ND, int NFC, typename R>
+struct Carry
+{
+    R mm[ND];
+    R mb[ND];
+    R p[NFC][ND + 2];
+    R q[NFC][ND + 2];
+};
+
+// Face means of mid and dB (FP32 geometry; zero with FP64 geometry).
+template <int CT, typename R, typename G>
+__device__ __forceinline__ void face_means(MarchArgs<R, G> const & a, int64_t icl, R * mm, R * mb)
+{
+    constexpr int ND = CellT<CT>::ND;
+    constexpr int NFC = CellT<CT>::NFC;
+    using D = Geo<ND, G>;
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+    {
+        mm[d] = R(0);
+        mb[d] = R(0);
+    }
+    if constexpr (D::MID)
+    {
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                mm[d] += fg<ND>(a, f, D::K_MID + d, icl);
+                mb[d] += fg<ND>(a, f, D::K_DB + d, icl);
+            }
+        }
+        R const inv = R(1) / R(NFC);
+#pragma unroll
+        for (int d = 0; d < ND; ++d)
+        {
+            mm[d] *= inv;
+            mb[d] *= inv;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // calc_soln for one body cell (euler_march.cpp:197-303): the CESE flux
 // integral over the cell's BCEs, divided by the CCE volume.
@@ -130,7 +185,8 @@ __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t
 // With CACHE set (the fused march, where every record's primitive cache is
 // valid) a neighbour's primitives come from its record.
 template <int CT, typename R, typename G, bool CACHE = false>
-__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n)
+__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n,
+                                          Carry<CellT<CT>::ND, CellT<CT>::NFC, R> * carry = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -158,6 +214,38 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
             dB[d] = fg<ND>(a, f, D::K_DB + d, icl);
             nh[d] = fg<ND>(a, f, D::K_NH + d, icl);
             qn[d] = a.qdt * nh[d];
+        }
+        if (carry)
+        {
+            R A[ND], B[ND];
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+            {
+                if constexpr (D::MID)
+                {
+                    A[d] = dB[d] - carry->mm[d];
+                    B[d] = carry->mb[d] - dB[d];
+                }
+                else
+                {
+                    A[d] = fg<ND>(a, f, D::K_R + d, icl);
+                    B[d] = fg<ND>(a, f, D::K_Q + d, icl);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                R pp = u[i] + a.hdt * t[i];
+                R qq = R(0);
+#pragma unroll
+                for (int d = 0; d < ND; ++d)
+                {
+                    pp += A[d] * g[i * ND + d];
+                    qq += B[d] * g[i * ND + d];
+                }
+                carry->p[f][i] = pp;
+                carry->q[f][i] = qq;
+            }
         }
         // Spatial flux: neighbour solution at the BCE centroid times its volume.
 #pragma unroll
@@ -260,10 +348,12 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 // solve, W-1/2 weights, W-3/4 cap, weighted sum.  The neighbour records are
 // gathered a second time (calc_soln just read them, so the loads hit in
 // cache); carrying calc_soln's neighbour terms over instead costs more FP64
-// operations and, in FP32, twice the registers and half the occupancy.
+// operations and, in 2D FP32, registers and occupancy.  FP32 tetrahedra do
+// carry them (carry != nullptr, see Carry).
 template <int CT, typename R, typename G>
 __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
-                                           R * so1n)
+                                           R * so1n,
+                                           Carry<CellT<CT>::ND, CellT<CT>::NFC, R> const * carry = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -281,31 +371,18 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     // here from the face means (the faces' values are read again rather than
     // held: they hit in L1, and registers bound this kernel's occupancy).
     R mm[ND], mb[ND];
-#pragma unroll
-    for (int d = 0; d < ND; ++d)
+    if (carry)
     {
-        mm[d] = R(0);
-        mb[d] = R(0);
-    }
-    if constexpr (D::MID)
-    {
-#pragma unroll
-        for (int f = 0; f < NFC; ++f)
-        {
-#pragma unroll
-            for (int d = 0; d < ND; ++d)
-            {
-                mm[d] += fg<ND>(a, f, D::K_MID + d, icl);
-                mb[d] += fg<ND>(a, f, D::K_DB + d, icl);
-            }
-        }
-        R const inv = R(1) / R(NFC);
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
-            mm[d] *= inv;
-            mb[d] *= inv;
+            mm[d] = carry->mm[d];
+            mb[d] = carry->mb[d];
         }
+    }
+    else
+    {
+        face_means<CT, R, G>(a, icl, mm, mb);
     }
     R idis[NFC][ND];
 #pragma unroll
@@ -374,36 +451,51 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 
     // Solution deltas at the evaluation points: uf[f][i].
     R uf[NFC][NEQ];
-#pragma unroll
-    for (int f = 0; f < NFC; ++f)
+    if (carry)
     {
-        int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
-        R rec[Rec<ND, R>::NUSED];
-        load_rec<ND, R>(a.cur + jr * Rec<ND, R>::RS, rec);
-        R jd[ND];
 #pragma unroll
-        for (int d = 0; d < ND; ++d)
+        for (int f = 0; f < NFC; ++f)
         {
-            if constexpr (D::MID)
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
             {
-                R const db = fg<ND>(a, f, D::K_DB + d, icl);
-                jd[d] = (db - mm[d]) + tau * (mb[d] - db) - delta[d];
-            }
-            else
-            {
-                jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+                uf[f][i] = (carry->p[f][i] + tau * carry->q[f][i]) - so0n[i];
             }
         }
+    }
+    else
+    {
 #pragma unroll
-        for (int i = 0; i < NEQ; ++i)
+        for (int f = 0; f < NFC; ++f)
         {
-            R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
+            int64_t const jr = ldg(a.nbr + f * a.ncell + icl);
+            R rec[Rec<ND, R>::NUSED];
+            load_rec<ND, R>(a.cur + jr * Rec<ND, R>::RS, rec);
+            R jd[ND];
 #pragma unroll
             for (int d = 0; d < ND; ++d)
             {
-                s += jd[d] * rec[2 * NEQ + i * ND + d];
+                if constexpr (D::MID)
+                {
+                    R const db = fg<ND>(a, f, D::K_DB + d, icl);
+                    jd[d] = (db - mm[d]) + tau * (mb[d] - db) - delta[d];
+                }
+                else
+                {
+                    jd[d] = fg<ND>(a, f, D::K_R + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl) - delta[d];
+                }
             }
-            uf[f][i] = s;
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
+#pragma unroll
+                for (int d = 0; d < ND; ++d)
+                {
+                    s += jd[d] * rec[2 * NEQ + i * ND + d];
+                }
+                uf[f][i] = s;
+            }
         }
     }
 
@@ -750,8 +842,16 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     constexpr int NFC = CellT<CT>::NFC;
     int64_t const row = icl + a.ngst;
 
+    // FP32 tetrahedra hand calc_soln's neighbour terms to calc_dsoln instead
+    // of gathering the neighbour records again (see Carry).
+    constexpr bool CARRY = sizeof(R) == 4 && CellT<CT>::SIMPLEX && ND == 3;
+    Carry<ND, NFC, R> carry;
+    if constexpr (CARRY)
+    {
+        face_means<CT, R, G>(a, icl, carry.mm, carry.mb);
+    }
     R so0n[NEQ];
-    soln_cell<CT, R, G, true>(a, icl, so0n);
+    soln_cell<CT, R, G, true>(a, icl, so0n, CARRY ? &carry : nullptr);
 
     // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
 #pragma unroll
@@ -778,7 +878,7 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     R rinv;
     R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n, rinv);
     R so1n[NEQ * ND];
-    dsoln_cell<CT, R, G>(a, icl, so0n, cflc, so1n);
+    dsoln_cell<CT, R, G>(a, icl, so0n, cflc, so1n, CARRY ? &carry : nullptr);
     R so0t[NEQ];
     Prim<ND, R> const q(so0n, ldg(a.gamma + row), rinv);
     solt_prim<ND, R>(q, so0n, so1n, so0t);
@@ -842,13 +942,15 @@ __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
     fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
-// The same kernel asking the compiler for 5 resident blocks of 128 (at most
-// 102 registers): the 3D FP32 tetrahedron kernel, latency-bound at the 4
-// blocks its 106 registers allow, measured 4.7% faster so (more blocks
-// spill).  A stated minimum of 1 would instead free the compiler to use up
-// to 255 registers, so the other kernels keep the one-argument bound.
+// The same kernel asking the compiler for 4 resident blocks of 128 (at most
+// 128 registers): the 3D FP32 tetrahedron kernel, which carries calc_soln's
+// neighbour terms to calc_dsoln in registers.  Measured at 24.6M cells: 4.66
+// ms per launch against 4.75 ms at 5 blocks (96 registers and spills) and
+// 5.92 ms for the form that gathers the neighbour records twice.  A stated
+// minimum of 1 would instead free the compiler to use up to 255 registers,
+// so the other kernels keep the one-argument bound.
 template <int ND, typename R, typename G, int CT1>
-__global__ void __launch_bounds__(128, 5) k_fused_5(MarchArgs<R, G> a)
+__global__ void __launch_bounds__(128, 4) k_fused_4(MarchArgs<R, G> a)
 {
     fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
