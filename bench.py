@@ -58,7 +58,7 @@ ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
 # (192 B instead of 128 B), which trades DRAM bytes, idle in the FP64-bound
 # march, for FP64 operations.
 NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 769.5, ("tri2d", "fp32"): 270.2,
-                        ("tet3d", "fp64"): 1337.3, ("tet3d", "fp32"): 626.2}
+                        ("tet3d", "fp64"): 1337.3, ("tet3d", "fp32"): 627.1}
 NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1159.6, ("tet3d", "fp64"): 2717.4}
 
 WORKLOADS = {
