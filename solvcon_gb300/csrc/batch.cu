@@ -35,7 +35,7 @@ using scg::dev::MarchArgs;
 // the single-core kernel reads its parameters, instead of being held in
 // registers.
 template <int ND, typename R, typename G, int B, int CT1>
-__global__ void __launch_bounds__(B) k_fused_batch(MarchArgs<R, G> const * descs, int2 const * tiles, int ntiles)
+__device__ __forceinline__ void fused_batch_tiles(MarchArgs<R, G> const * descs, int2 const * tiles, int ntiles)
 {
     using Args = MarchArgs<R, G>;
     static_assert(sizeof(Args) % sizeof(int) == 0, "argument block is whole words");
@@ -53,6 +53,48 @@ __global__ void __launch_bounds__(B) k_fused_batch(MarchArgs<R, G> const * descs
         }
         __syncthreads();
         scg::dev::fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(tl.y) + threadIdx.x);
+    }
+}
+
+template <int ND, typename R, typename G, int B, int CT1>
+__global__ void __launch_bounds__(B) k_fused_batch(MarchArgs<R, G> const * descs, int2 const * tiles, int ntiles)
+{
+    fused_batch_tiles<ND, R, G, B, CT1>(descs, tiles, ntiles);
+}
+
+// The same with the resident-block request of the single-core kernel whose
+// cells carry calc_soln's neighbour terms (scg::dev::min_blocks).
+template <int ND, typename R, typename G, int B, int CT1, int MINB>
+__global__ void __launch_bounds__(B, MINB) k_fused_batch_mb(MarchArgs<R, G> const * descs, int2 const * tiles,
+                                                            int ntiles)
+{
+    fused_batch_tiles<ND, R, G, B, CT1>(descs, tiles, ntiles);
+}
+
+template <int ND, typename R, typename G, int B, int CT1>
+constexpr int batch_min_blocks()
+{
+    if constexpr (CT1 == 0)
+    {
+        return 0;
+    }
+    else
+    {
+        return scg::dev::min_blocks<ND, R, CT1, B>();
+    }
+}
+
+template <int ND, typename R, typename G, int B, int CT1>
+constexpr auto batch_kernel()
+{
+    constexpr int MINB = batch_min_blocks<ND, R, G, B, CT1>();
+    if constexpr (MINB > 0)
+    {
+        return &k_fused_batch_mb<ND, R, G, B, CT1, MINB>;
+    }
+    else
+    {
+        return &k_fused_batch<ND, R, G, B, CT1>;
     }
 }
 
@@ -113,7 +155,7 @@ public:
         int dev = 0, nsm = 0, occ = 0;
         scg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
         scg::cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
-        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_fused_batch<ND, R, G, B, CT1>, B, 0),
+        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<ND, R, G, B, CT1>(), B, 0),
                         "occupancy");
         int64_t const resident = static_cast<int64_t>(nsm) * std::max(occ, 1);
         grid = persistent ? std::min<int64_t>(ntiles, resident) : ntiles;
@@ -164,7 +206,7 @@ public:
     {
         for (int p = 0; p < 2; ++p)
         {
-            k_fused_batch<ND, R, G, B, CT1><<<static_cast<unsigned>(grid), B, 0, stream>>>(
+            batch_kernel<ND, R, G, B, CT1>()<<<static_cast<unsigned>(grid), B, 0, stream>>>(
                 descs[p].ptr, tiles.ptr, static_cast<int>(ntiles));
             scg::launched(stream, "fused_batch");
         }

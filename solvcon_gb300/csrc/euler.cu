@@ -1219,9 +1219,10 @@ public:
         constexpr int SIMPLEX = (ND == 2) ? CT_TRIANGLE : CT_TET;
         if (single_ct == SIMPLEX)
         {
-            if constexpr (ND == 3 && sizeof(R) == 4)
+            constexpr int MINB = min_blocks<ND, R, SIMPLEX, BLOCK>();
+            if constexpr (MINB > 0)
             {
-                k_fused_4<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+                k_fused_mb<ND, R, G, SIMPLEX, MINB><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
             }
             else
             {

@@ -124,16 +124,44 @@ __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t
 }
 
 // What calc_soln hands to calc_dsoln of the same cell when the neighbour
-// records are not gathered twice (FP32 tetrahedra, whose four 128-byte
-// neighbour records cost more to gather again than 40 registers cost to
-// keep; in 2D the extra registers lose more occupancy than the second
-// gather costs, measured 4% slower): the solution change at
+// records are not gathered twice (FP32 triangles and tetrahedra; see
+// min_blocks for the register budget that makes it pay): the solution change at
 // face f's gradient-evaluation point is linear in tau,
 //   u_j + hdt ut_j + jdis . g_j - u_i  with  jdis = A_f + tau B_f,
 // so calc_soln, holding neighbour j's record, keeps
 //   p[f] = u_j + hdt ut_j + A_f . g_j  and  q[f] = B_f . g_j
 // per equation.  A_f = dB_f - mean(mid), B_f = mean(dB) - dB_f with FP32
 // geometry (R_f and Q_f with FP64 geometry); delta is zero for simplices.
+// Whether the fused substep of cell type CT carries calc_soln's neighbour
+// terms to calc_dsoln (FP32 simplices) instead of gathering again.
+template <typename R, int CT>
+__host__ __device__ constexpr bool carries()
+{
+    return sizeof(R) == 4 && CellT<CT>::SIMPLEX;
+}
+
+// Resident blocks of `block` threads to ask of the compiler for a fused
+// kernel whose cells carry (0: keep the one-argument launch bound).  The
+// carried sums hold 24 (2D) / 40 (3D) more floats; measured at 128 threads,
+// 2M triangles: 0.1727 ms per launch without carrying (64 registers), with
+// carrying 0.1771 ms at 5 blocks (96 registers), 0.1662 at 6, 0.1555 at 7
+// (72 registers, 28 bytes spilled), 0.1557 at 8 (64 registers, 60 bytes
+// spilled); 24.6M tetrahedra: 5.92 ms without, 4.75 ms at 5 blocks (96
+// registers, 80 bytes spilled), 4.66 ms at 4 (128 registers).  The budget
+// per thread (72 / 128 registers) is kept for other block sizes.
+template <int ND, typename R, int CT, int BLOCK>
+__host__ __device__ constexpr int min_blocks()
+{
+    if constexpr (!carries<R, CT>())
+    {
+        return 0;
+    }
+    else
+    {
+        return 65536 / (BLOCK * (ND == 2 ? 72 : 128));
+    }
+}
+
 template <int ND, int NFC, typename R>
 struct Carry
 {
@@ -348,8 +376,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 // solve, W-1/2 weights, W-3/4 cap, weighted sum.  The neighbour records are
 // gathered a second time (calc_soln just read them, so the loads hit in
 // cache); carrying calc_soln's neighbour terms over instead costs more FP64
-// operations and, in 2D FP32, registers and occupancy.  FP32 tetrahedra do
-// carry them (carry != nullptr, see Carry).
+// operations, but pays in FP32 for simplices (carry != nullptr, see Carry).
 template <int CT, typename R, typename G>
 __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
                                            R * so1n,
@@ -842,9 +869,9 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     constexpr int NFC = CellT<CT>::NFC;
     int64_t const row = icl + a.ngst;
 
-    // FP32 tetrahedra hand calc_soln's neighbour terms to calc_dsoln instead
+    // FP32 simplices hand calc_soln's neighbour terms to calc_dsoln instead
     // of gathering the neighbour records again (see Carry).
-    constexpr bool CARRY = sizeof(R) == 4 && CellT<CT>::SIMPLEX && ND == 3;
+    constexpr bool CARRY = carries<R, CT>();
     Carry<ND, NFC, R> carry;
     if constexpr (CARRY)
     {
@@ -942,15 +969,12 @@ __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
     fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
-// The same kernel asking the compiler for 4 resident blocks of 128 (at most
-// 128 registers): the 3D FP32 tetrahedron kernel, which carries calc_soln's
-// neighbour terms to calc_dsoln in registers.  Measured at 24.6M cells: 4.66
-// ms per launch against 4.75 ms at 5 blocks (96 registers and spills) and
-// 5.92 ms for the form that gathers the neighbour records twice.  A stated
-// minimum of 1 would instead free the compiler to use up to 255 registers,
-// so the other kernels keep the one-argument bound.
-template <int ND, typename R, typename G, int CT1>
-__global__ void __launch_bounds__(128, 4) k_fused_4(MarchArgs<R, G> a)
+// The same kernel asking the compiler for MINB resident blocks of 128
+// (min_blocks).  A stated minimum of 1 would instead free the compiler to use
+// up to 255 registers, so the kernels that do not carry keep the one-argument
+// bound.
+template <int ND, typename R, typename G, int CT1, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_fused_mb(MarchArgs<R, G> a)
 {
     fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
