@@ -602,9 +602,9 @@ def dt_for_cfl_g(mesh, state, cfl, gamma):
 
 
 def run_batch(args, world, rank, dist):
-    """Config 4: one FP32 batched march of many meshes (autotuned tile and
-    grid policy, CUDA graph per step) against the same meshes marched one
-    after the other in plain FP64."""
+    """The batched workload: one FP32 batched march of many meshes
+    (autotuned tile and grid policy, CUDA graph per step) against the same
+    meshes marched one after the other in plain FP64."""
     from solvcon_gb300._lib import launch_count
     from solvcon_gb300.batch import EulerBatch, autotune
     nmesh = args.nmesh
@@ -712,11 +712,11 @@ def run_batch(args, world, rank, dist):
 
 
 def run_serve(args, world, rank, dist):
-    """Config 5: Poisson arrivals of mixed 1D tubes (30%) and 2D meshes
-    (70%, the batched workload's distribution), 200-2000 steps each, served
-    with continuous batching under a 120 GB HBM budget; p50/p99 latency and
-    aggregate cell-steps/s per arrival rate, against each request marched
-    alone with the plain FP64 march."""
+    """The served workload: Poisson arrivals of mixed 1D tubes (30%) and 2D
+    meshes (70%, the batched workload's distribution), 200-2000 steps each,
+    served with continuous batching under a 120 GB HBM budget; p50/p99
+    latency and aggregate cell-steps/s per arrival rate, against each
+    request marched alone with the plain FP64 march."""
     from solvcon_gb300 import serving
     nreq = args.nreq
     data = batch_meshes(args.nmesh, seed=4242 + 1000 * rank)
