@@ -558,24 +558,42 @@ def run_line(args, world, rank, dist):
         print(json.dumps(line), flush=True)
 
 
-def batch_meshes(nmesh, seed=2026, lo=2000, hi=200000):
-    """The batched workload: nmesh jittered triangulated squares with cell
-    counts log-uniform in [lo, hi], per-mesh four-quadrant states and gamma
-    in [1.1, 1.67], slip walls."""
-    from solvcon_gb300 import meshgen
+def _batch_params(nmesh, seed, lo, hi):
     rng = np.random.Generator(np.random.PCG64(seed))
     ncells = np.exp(rng.uniform(np.log(lo), np.log(hi), nmesh))
     gammas = rng.uniform(1.1, 1.67, nmesh)
-    out = []
-    for k in range(nmesh):
-        nside = max(2, int(round(np.sqrt(ncells[k] / 2.0))))
-        x, t, c = meshgen.tri_square(nside, 0.2, seed + 1 + k)
-        mesh = meshgen.build_mesh(2, x, t, c)
-        clcnd = np.asarray(mesh.clcnd.ndarray)[mesh.ngstcell:]
-        state = meshgen.quadrant_state(clcnd, seed + 1 + k, gammas[k])
-        faces = np.asarray(mesh.bndfcs.ndarray[:, 0]).copy()
-        out.append((mesh, state, faces, float(gammas[k])))
-    return out
+    return ncells, gammas
+
+
+def batch_mesh(k, ncell, gamma, seed, order="native"):
+    """Mesh k of the batched workload: a jittered triangulated square of
+    about ``ncell`` cells, its four-quadrant state, slip-wall faces and
+    gamma.  ``order="morton"`` numbers its cells along a Z-order curve of
+    their node averages (the same mesh and state, renumbered)."""
+    from solvcon_gb300 import meshgen
+    from solvcon_gb300.batch import morton_order, node_average
+    nside = max(2, int(round(np.sqrt(ncell / 2.0))))
+    x, t, c = meshgen.tri_square(nside, 0.2, seed + 1 + k)
+    if order == "morton":
+        p = morton_order(node_average(x, c))
+        t, c = np.asarray(t)[p], np.asarray(c)[p]
+    elif order != "native":
+        raise ValueError("unknown cell order %r" % order)
+    mesh = meshgen.build_mesh(2, x, t, c)
+    clcnd = np.asarray(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    state = meshgen.quadrant_state(clcnd, seed + 1 + k, gamma)
+    faces = np.asarray(mesh.bndfcs.ndarray[:, 0]).copy()
+    return mesh, state, faces, float(gamma)
+
+
+def batch_meshes(nmesh, seed=2026, lo=2000, hi=200000, order="native",
+                 only=None):
+    """The batched workload: nmesh jittered triangulated squares with cell
+    counts log-uniform in [lo, hi], per-mesh four-quadrant states and gamma
+    in [1.1, 1.67], slip walls (``only``: the indices to build)."""
+    ncells, gammas = _batch_params(nmesh, seed, lo, hi)
+    ks = range(nmesh) if only is None else only
+    return [batch_mesh(k, ncells[k], gammas[k], seed, order) for k in ks]
 
 
 def setup_core_g(mesh, state, faces, dt, precision, gamma):
@@ -603,28 +621,38 @@ def dt_for_cfl_g(mesh, state, cfl, gamma):
 
 def run_batch(args, world, rank, dist):
     """The batched workload: one FP32 batched march of many meshes
-    (autotuned tile and grid policy, CUDA graph per step) against the same
-    meshes marched one after the other in plain FP64."""
+    (autotuned tile, grid policy and cell ordering, CUDA graph per step)
+    against the same meshes marched one after the other in plain FP64."""
     from solvcon_gb300._lib import launch_count
     from solvcon_gb300.batch import EulerBatch, autotune
     nmesh = args.nmesh
-    t_setup = time.perf_counter()
-    data = batch_meshes(nmesh, seed=2026 + 1000 * rank)
-    dts = [dt_for_cfl_g(m, s, 0.8, g) for m, s, f, g in data]
+    seed = 2026 + 1000 * rank
     prec = args.precision or "fp32"
+
+    # Autotune tile, grid policy and cell ordering on scratch cores of a
+    # subset of the meshes, each built in both cell orders.
+    t_tune = time.perf_counter()
+    sub = list(range(0, nmesh, max(1, nmesh // 32)))
+    cand = {}
+    for order in ("native", "morton"):
+        cand[order] = [setup_core_g(m, s, f, dt_for_cfl_g(m, s, 0.8, g),
+                                    prec, g)
+                       for m, s, f, g in batch_meshes(nmesh, seed,
+                                                      order=order, only=sub)]
+    best, table = autotune(cand["native"], steps=2, repeat=2,
+                           orderings={"morton": cand["morton"]})
+    del cand
+    t_tune = time.perf_counter() - t_tune
+
+    t_setup = time.perf_counter()
+    data = batch_meshes(nmesh, seed, order=best["ordering"])
+    dts = [dt_for_cfl_g(m, s, 0.8, g) for m, s, f, g in data]
     fast = [setup_core_g(m, s, f, dt, prec, g)
             for (m, s, f, g), dt in zip(data, dts)]
     plain = [setup_core_g(m, s, f, dt, "fp64", g)
              for (m, s, f, g), dt in zip(data, dts)]
     t_setup = time.perf_counter() - t_setup
     ncell = sum(c.ncell for c in fast)
-
-    # Autotune on scratch copies of a subset, then batch every core.
-    sub = list(range(0, nmesh, max(1, nmesh // 32)))
-    scratch = [setup_core_g(data[k][0], data[k][1], data[k][2], dts[k], prec,
-                            data[k][3]) for k in sub]
-    best, table = autotune(scratch, steps=2, repeat=2)
-    del scratch
     batch = EulerBatch(fast, block=best["block"],
                        persistent=best["persistent"])
     batch.march(args.warmup)
@@ -694,6 +722,7 @@ def run_batch(args, world, rank, dist):
                                "0.8, slip walls)" % (nmesh, nmesh),
                    "cells": ncell, "meshes": nmesh, "precision": prec,
                    "autotune": best, "autotune_table": table,
+                   "autotune_s": t_tune,
                    "l2": "state larger than L2 (no flush needed)",
                    "setup_s": t_setup},
         "baseline_plain_fp64_sequential": {

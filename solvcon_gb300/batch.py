@@ -9,7 +9,9 @@ bit-identical to marching it alone.
 
 :func:`autotune` picks the tile (block) size, the grid policy (persistent
 blocks striding over the work list, or one block per tile) and, when given
-alternatives, the cell ordering, by timing a few steps of each candidate.
+the same meshes in other cell orders (e.g. :func:`morton_order` of
+:func:`node_average`), the cell ordering, by timing a few steps of each
+candidate.
 """
 
 import ctypes
@@ -20,7 +22,7 @@ import numpy as np
 from . import _lib
 from ._lib import check, ptr
 
-__all__ = ["EulerBatch", "autotune", "morton_order"]
+__all__ = ["EulerBatch", "autotune", "morton_order", "node_average"]
 
 _vp = ctypes.c_void_p
 lib = _lib.bind_more({
@@ -95,25 +97,45 @@ def morton_order(points):
     return np.argsort(code, kind="stable")
 
 
+def node_average(ndcrd, clnds):
+    """Node average of every cell (clnds rows: count, then node ids), the
+    point a cell ordering sorts by."""
+    x = np.asarray(ndcrd, dtype="float64")
+    c = np.asarray(clnds)
+    n = c[:, 0].astype("int64")
+    out = np.zeros((len(c), x.shape[1]))
+    for k in range(1, c.shape[1]):
+        has = n >= k
+        out[has] += x[c[has, k]]
+    return out / n[:, None]
+
+
 def autotune(cores, steps=2, blocks=(64, 128, 256),
-             persistents=(True, False), repeat=2):
+             persistents=(True, False), repeat=2, orderings=None):
     """Time each (block, persistent) candidate on ``cores``; return the
     fastest configuration and the table of timings (ms per step).
 
-    The cores are marched ``(1 + repeat) * steps`` steps per candidate, so
-    pass scratch copies when their state matters."""
+    ``orderings`` optionally maps a name to the same meshes with their cells
+    in another order (``cores`` are "native"); every (ordering, block,
+    persistent) candidate is timed and the fastest one's ordering is
+    returned with it.  The cores are marched ``(1 + repeat) * steps`` steps
+    per candidate, so pass scratch copies when their state matters."""
+    sets = {"native": cores}
+    sets.update(orderings or {})
     table = []
-    for block in blocks:
-        for pers in persistents:
-            b = EulerBatch(cores, block=block, persistent=pers)
-            b.march(steps)  # warm-up (graph capture)
-            best = float("inf")
-            for _ in range(repeat):
-                b.march(steps)
-                best = min(best, b.last_ms / steps)
-            table.append({"block": block, "persistent": pers,
-                          "ms_per_step": best, "grid": b.grid})
-            del b
+    for name, cs in sets.items():
+        for block in blocks:
+            for pers in persistents:
+                b = EulerBatch(cs, block=block, persistent=pers)
+                b.march(steps)  # warm-up (graph capture)
+                best = float("inf")
+                for _ in range(repeat):
+                    b.march(steps)
+                    best = min(best, b.last_ms / steps)
+                table.append({"ordering": name, "block": block,
+                              "persistent": pers, "ms_per_step": best,
+                              "grid": b.grid})
+                del b
     fastest = min(table, key=lambda r: r["ms_per_step"])
     return fastest, table
 

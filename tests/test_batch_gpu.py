@@ -84,6 +84,39 @@ def test_autotune_candidates_agree():
     cores = _cores(2, "fp32", seeds)
     best, table = autotune([c for _, c in cores], steps=1, repeat=1)
     assert len(table) == 6 and best["ms_per_step"] > 0
+    assert best["ordering"] == "native"
+    other = _cores(2, "fp32", seeds)
+    best, table = autotune([c for _, c in cores], steps=1, repeat=1,
+                           blocks=(64,), persistents=(True,),
+                           orderings={"again": [c for _, c in other]})
+    assert [r["ordering"] for r in table] == ["native", "again"]
+    assert best["ordering"] in ("native", "again")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_cell_renumbering_leaves_the_march_unchanged(precision):
+    """The same mesh with its cells in Morton order marches to the same
+    state, cell for cell: each cell's arithmetic (its faces in its own node
+    order, its neighbours' records) does not depend on the numbering."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__))))
+    import bench
+    from solvcon_gb300.batch import EulerBatch
+    got = {}
+    for order in ("native", "morton"):
+        m, s, f, g = bench.batch_mesh(5, 3000, 1.4, 2026, order)
+        dt = bench.dt_for_cfl_g(m, s, 0.8, g)
+        c = bench.setup_core_g(m, s, f, dt, precision, g)
+        EulerBatch([c], block=64).march(5)
+        cl = np.array(m.clnds.ndarray)[m.ngstcell:, :4]
+        got[order] = (cl, np.array(c.so0n.ndarray)[c.ngstcell:],
+                      np.array(c.so1n.ndarray)[c.ngstcell:])
+    key = {tuple(r): i for i, r in enumerate(got["native"][0].tolist())}
+    perm = np.array([key[tuple(r)] for r in got["morton"][0].tolist()])
+    for k in (1, 2):
+        np.testing.assert_array_equal(got["morton"][k], got["native"][k][perm])
 
 
 def test_batch_rejects_mixed_cores():

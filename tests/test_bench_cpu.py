@@ -55,3 +55,23 @@ def test_reference_arm_line_spacetime():
     line = _reference_line("--workload", "spacetime", "--cpu-nside", "500")
     assert line["metric"] == "point-steps/s" and line["value"] > 0
     assert line["config"]["sample_units"] == 2 * 500 + 1
+
+
+def test_batch_mesh_morton_is_a_renumbering():
+    """The batched workload's Morton cell order renumbers the same mesh: the
+    same cells (as node lists), the same state per cell."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    a = bench.batch_mesh(3, 900, 1.3, 2026, "native")
+    b = bench.batch_mesh(3, 900, 1.3, 2026, "morton")
+    ma, mb = a[0], b[0]
+    assert ma.ncell == mb.ncell and ma.nface == mb.nface
+    ca = np.array(ma.clnds.ndarray)[ma.ngstcell:, :4]
+    cb = np.array(mb.clnds.ndarray)[mb.ngstcell:, :4]
+    key = {tuple(r): i for i, r in enumerate(ca.tolist())}
+    perm = np.array([key[tuple(r)] for r in cb.tolist()])
+    assert sorted(perm.tolist()) == list(range(ma.ncell))
+    assert not np.array_equal(perm, np.arange(ma.ncell))
+    np.testing.assert_array_equal(b[1], a[1][perm])
+    assert a[3] == b[3] and len(a[2]) == len(b[2])
