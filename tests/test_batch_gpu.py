@@ -96,8 +96,11 @@ def test_autotune_candidates_agree():
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_cell_renumbering_leaves_the_march_unchanged(precision):
     """The same mesh with its cells in Morton order marches to the same
-    state, cell for cell: each cell's arithmetic (its faces in its own node
-    order, its neighbours' records) does not depend on the numbering."""
+    state, cell for cell, to round-off: each cell sums over its faces in its
+    own node order, but a shared face belongs to (and its geometry is
+    computed from) the lower-numbered of its two cells, so the geometry's
+    rounding follows the numbering (measured: 1.4e-14 absolute in FP64
+    after 5 steps)."""
     import sys
     import os
     sys.path.insert(0, os.path.dirname(os.path.dirname(
@@ -115,8 +118,11 @@ def test_cell_renumbering_leaves_the_march_unchanged(precision):
                       np.array(c.so1n.ndarray)[c.ngstcell:])
     key = {tuple(r): i for i, r in enumerate(got["native"][0].tolist())}
     perm = np.array([key[tuple(r)] for r in got["morton"][0].tolist()])
+    tol = 1e-12 if precision == "fp64" else 2e-5
     for k in (1, 2):
-        np.testing.assert_array_equal(got["morton"][k], got["native"][k][perm])
+        want = got["native"][k][perm]
+        np.testing.assert_allclose(got["morton"][k], want, rtol=0,
+                                   atol=tol * np.abs(want).max())
 
 
 def test_batch_rejects_mixed_cores():
