@@ -345,6 +345,82 @@ __global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int o
     rec[r1 * Rec<ND, R>::RS + off + k1] = R(v.y);
 }
 
+// so1n written from a mapped host table and then calc_solt of each row as
+// it now stands (its so0 already in the record): the next march finds so0t
+// and the FP64 primitive cache of the new state made, and the Jacobian
+// products run while other blocks wait on the host link.  A block copies its
+// rows' contiguous stretch of the host table to shared memory in 16-byte
+// pieces (vec: the table is 16-byte aligned; a block's stretch starts at a
+// multiple of 128 rows, so it is aligned too), then one thread per row
+// finishes the row.  The values and the arithmetic are those of
+// k_set_field_host followed by k_solt_rows.
+template <int ND, typename R>
+__global__ void __launch_bounds__(BLOCK) k_set_so1_host_solt(R * rec, double const * in, R const * gamma,
+                                                             int64_t nrow, bool vec)
+{
+    constexpr int NEQ = ND + 2;
+    constexpr int W = NEQ * ND;
+    using RC = Rec<ND, R>;
+    __shared__ double buf[BLOCK * W];
+    int64_t const r0 = static_cast<int64_t>(blockIdx.x) * BLOCK;
+    int64_t const left = nrow - r0;
+    int const nr = static_cast<int>(left < BLOCK ? left : BLOCK);
+    int const n = nr * W;
+    double const * const src = in + r0 * W;
+    for (int i = 2 * static_cast<int>(threadIdx.x); i < n; i += 2 * BLOCK)
+    {
+        if (vec && i + 1 < n)
+        {
+            double2 const v = *reinterpret_cast<double2 const *>(src + i);
+            buf[i] = v.x;
+            buf[i + 1] = v.y;
+        }
+        else
+        {
+            buf[i] = src[i];
+            if (i + 1 < n)
+            {
+                buf[i + 1] = src[i + 1];
+            }
+        }
+    }
+    __syncthreads();
+    if (static_cast<int>(threadIdx.x) >= nr)
+    {
+        return;
+    }
+    int64_t const r = r0 + threadIdx.x;
+    R * const row = rec + r * RC::RS;
+    R v[RC::NUSED];
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        v[i] = row[i];
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+    {
+        v[2 * NEQ + k] = R(buf[threadIdx.x * W + k]);
+    }
+    Prim<ND, R> const q(v, gamma[r]);
+    R t[NEQ];
+    solt_prim<ND, R>(q, v, v + 2 * NEQ, t);
+#pragma unroll
+    for (int i = 0; i < NEQ; ++i)
+    {
+        row[NEQ + i] = t[i];
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+    {
+        row[2 * NEQ + k] = v[2 * NEQ + k];
+    }
+    if constexpr (RC::PRIM)
+    {
+        q.cache(row + RC::OP);
+    }
+}
+
 template <typename R>
 __global__ void k_to_f64(R const * in, double * out, int64_t n)
 {
@@ -1022,10 +1098,23 @@ public:
                 R * base;
                 int off, width;
                 field_of(which, base, off, width);
-                k_set_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
-                    base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
-                launched(stream, "set_field_host");
-                next_valid = false;
+                if (which == EA_SO1N && tbuf != (cur ^ 1))
+                {
+                    // The new state's so0t can go into its record (the
+                    // logical so0t lives in the other buffer): make it now.
+                    k_set_so1_host_solt<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(
+                        base, dev, d_gamma.ptr, nrow, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                    launched(stream, "set_so1_host_solt");
+                    next_valid = true;
+                    next_buf = cur ^ 1;
+                }
+                else
+                {
+                    k_set_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
+                        base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                    launched(stream, "set_field_host");
+                    next_valid = false;
+                }
                 sync();
                 return;
             }

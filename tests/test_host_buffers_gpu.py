@@ -116,6 +116,10 @@ def test_set_through_mapped_block_equals_staged(precision, ndim, skip):
             blk.free()
         np.testing.assert_array_equal(_get(b, which, new.shape),
                                       _get(a, which, new.shape), err_msg=name)
+        # so0t is untouched by either route (the mapped so1n route makes
+        # the new state's so0t in the record the march reads next).
+        np.testing.assert_array_equal(_get(b, 6, _shape(b, "so0t")),
+                                      _get(a, 6, _shape(a, "so0t")))
     a.march(2)
     b.march(2)
     for name in ("so0n", "so1n", "cflo"):
@@ -123,3 +127,33 @@ def test_set_through_mapped_block_equals_staged(precision, ndim, skip):
         shape = _shape(a, name)
         np.testing.assert_array_equal(_get(b, which, shape),
                                       _get(a, which, shape), err_msg=name)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_mapped_so1n_after_update_keeps_so0t(precision):
+    """After update() the logical so0t lives in the buffer so1n is written
+    to; the mapped route must then leave it alone."""
+    from solvcon_gb300._lib import check, lib, ptr
+    a = _marched_core(precision, 2)
+    b = _marched_core(precision, 2)
+    a.update()
+    b.update()
+    a.release_views()
+    b.release_views()
+    new = _get(a, 8, _shape(a, "so1n")) * 1.001
+    check(lib.scg_euler_set(a.handle, 8, ptr(new), new.size))
+    blk = _Block(new.size)
+    try:
+        blk.view[...] = new.ravel()
+        check(lib.scg_euler_set(b.handle, 8, ctypes.c_void_p(blk.addr),
+                                new.size))
+    finally:
+        blk.free()
+    for which, name in ((6, "so0t"), (8, "so1n"), (5, "so0n")):
+        np.testing.assert_array_equal(_get(b, which, _shape(b, name)),
+                                      _get(a, which, _shape(a, name)),
+                                      err_msg=name)
+    a.march(1)
+    b.march(1)
+    np.testing.assert_array_equal(_get(b, 5, _shape(b, "so0n")),
+                                  _get(a, 5, _shape(a, "so0n")))
