@@ -14,6 +14,7 @@
 #include "euler_core.hpp"
 #include "euler_kernels.cuh"
 #include "euler_setup.cuh"
+#include "reduce.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -488,13 +489,13 @@ __global__ void k_field(R const * nxt, R const * gamma, R const * cflo, int64_t 
 }
 
 // Per-block FP64 partial sums of so0n[:, i] * clvol (Kahan inside a thread,
-// tree across the block), and min/max of cflo.
+// warp shuffles across the block), and min/max of cflo.
 template <int ND, typename R>
-__global__ void k_totals(R const * nxt, double const * clvol, R const * cflo, int64_t ngst, int64_t ncell,
-                         double * part)
+__global__ void __launch_bounds__(BLOCK) k_totals(R const * nxt, double const * clvol, R const * cflo, int64_t ngst,
+                                                  int64_t ncell, double * part)
 {
     constexpr int NEQ = ND + 2;
-    __shared__ double sh[NEQ + 2][BLOCK];
+    __shared__ double sh[BLOCK / 32];
     double s[NEQ], c[NEQ];
     for (int i = 0; i < NEQ; ++i)
     {
@@ -518,31 +519,18 @@ __global__ void k_totals(R const * nxt, double const * clvol, R const * cflo, in
         lo = fmin(lo, cf);
         hi = fmax(hi, cf);
     }
+    double out[NEQ + 2];
     for (int i = 0; i < NEQ; ++i)
     {
-        sh[i][threadIdx.x] = s[i];
+        out[i] = red::block_fold<red::SUM, BLOCK / 32>(s[i], sh);
     }
-    sh[NEQ][threadIdx.x] = lo;
-    sh[NEQ + 1][threadIdx.x] = hi;
-    __syncthreads();
-    for (int w = BLOCK / 2; w > 0; w >>= 1)
-    {
-        if (threadIdx.x < w)
-        {
-            for (int i = 0; i < NEQ; ++i)
-            {
-                sh[i][threadIdx.x] += sh[i][threadIdx.x + w];
-            }
-            sh[NEQ][threadIdx.x] = fmin(sh[NEQ][threadIdx.x], sh[NEQ][threadIdx.x + w]);
-            sh[NEQ + 1][threadIdx.x] = fmax(sh[NEQ + 1][threadIdx.x], sh[NEQ + 1][threadIdx.x + w]);
-        }
-        __syncthreads();
-    }
+    out[NEQ] = red::block_fold<red::MIN, BLOCK / 32>(lo, sh);
+    out[NEQ + 1] = red::block_fold<red::MAX, BLOCK / 32>(hi, sh);
     if (threadIdx.x == 0)
     {
         for (int i = 0; i < NEQ + 2; ++i)
         {
-            part[blockIdx.x * (NEQ + 2) + i] = sh[i][0];
+            part[blockIdx.x * (NEQ + 2) + i] = out[i];
         }
     }
 }

@@ -861,7 +861,7 @@ __device__ __forceinline__ void bc1_ghost(int kind, double const * n, R const * 
 // substep for its own row and its ghost rows.  Reads only the current records
 // (neighbours' old values) and writes only rows it owns, so one launch covers
 // the whole substep with no grid-wide synchronisation.
-template <int CT, typename R, typename G, bool SPECIALISED = false>
+template <int CT, typename R, typename G>
 __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t icl)
 {
     constexpr int ND = CellT<CT>::ND;
@@ -871,9 +871,10 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
 
     // FP32 simplices hand calc_soln's neighbour terms to calc_dsoln instead
     // of gathering the neighbour records again (see Carry).
-    // (Only in the kernels compiled for one cell type, which ask for the
-    // register budget carrying needs; the mixed-type kernels gather twice.)
-    constexpr bool CARRY = SPECIALISED && carries<R, CT>();
+    // The choice depends on the cell type and precision only, never on the
+    // kernel, so a core's cells give the same bits in every kernel that
+    // marches them (single-type or mixed, alone or batched).
+    constexpr bool CARRY = carries<R, CT>();
     Carry<ND, NFC, R> carry;
     if constexpr (CARRY)
     {
@@ -927,7 +928,7 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
         if constexpr (CT1 != 0)
         {
             (void)ct;
-            fused_cell<CT1, R, G, true>(a, t);
+            fused_cell<CT1, R, G>(a, t);
         }
         else if constexpr (ND == 2)
         {

@@ -31,6 +31,7 @@
 
 #include "../../include/scg.h"
 #include "common.hpp"
+#include "reduce.cuh"
 #include "euler_core.hpp"
 
 #include <mutex>
@@ -71,13 +72,15 @@ double * scratch_for_current_device()
 }
 
 // Stage 1: block b sums cells [b * CHUNK, (b + 1) * CHUNK) of so0n * clvol
-// (compensated per thread, tree per block) and writes row b of the scratch.
-// Every row that stage 2 reads is rewritten here, so nothing needs clearing.
+// (compensated per thread, warp shuffles across the block) and writes row b
+// of the scratch.  Every row that stage 2 reads is rewritten here, so nothing
+// needs clearing.
 template <typename R>
-__global__ void k_totals_part(R const * rec, int rs, int neq, double const * clvol, int64_t ngst, int64_t ncell,
-                              double * scratch)
+__global__ void __launch_bounds__(TOTALS_THREADS) k_totals_part(R const * rec, int rs, int neq,
+                                                                double const * clvol, int64_t ngst, int64_t ncell,
+                                                                double * scratch)
 {
-    __shared__ double sh[TOTALS_ROW][TOTALS_THREADS];
+    __shared__ double sh[TOTALS_THREADS / 32];
     double s[5] = {0, 0, 0, 0, 0};
     double c[5] = {0, 0, 0, 0, 0};
     int64_t const begin = static_cast<int64_t>(blockIdx.x) * TOTALS_CHUNK;
@@ -96,25 +99,10 @@ __global__ void k_totals_part(R const * rec, int rs, int neq, double const * clv
     }
     for (int i = 0; i < neq; ++i)
     {
-        sh[i][threadIdx.x] = s[i];
-    }
-    __syncthreads();
-    for (int w = TOTALS_THREADS / 2; w > 0; w >>= 1)
-    {
-        if (threadIdx.x < w)
+        double const r = scg::red::block_fold<scg::red::SUM, TOTALS_THREADS / 32>(s[i], sh);
+        if (threadIdx.x == 0)
         {
-            for (int i = 0; i < neq; ++i)
-            {
-                sh[i][threadIdx.x] += sh[i][threadIdx.x + w];
-            }
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0)
-    {
-        for (int i = 0; i < neq; ++i)
-        {
-            scratch[blockIdx.x * TOTALS_ROW + i] = sh[i][0];
+            scratch[blockIdx.x * TOTALS_ROW + i] = r;
         }
     }
 }
