@@ -147,8 +147,10 @@ __host__ __device__ constexpr bool carries()
 // carrying 0.1771 ms at 5 blocks (96 registers), 0.1662 at 6, 0.1555 at 7
 // (72 registers, 28 bytes spilled), 0.1557 at 8 (64 registers, 60 bytes
 // spilled); 24.6M tetrahedra: 5.92 ms without, 4.75 ms at 5 blocks (96
-// registers, 80 bytes spilled), 4.66 ms at 4 (128 registers).  The budget
-// per thread (72 / 128 registers) is kept for other block sizes.
+// registers, 80 bytes spilled), 4.66 ms at 4 (128 registers).  With the
+// FP32 delta form (u0, d0 below) 7 blocks stay best in 2D (0.1628 ms; 6:
+// 0.1688, 8: 0.1683) and 4 in 3D (4.80 ms).  The budget per thread (72 /
+// 128 registers) is kept for other block sizes.
 template <int ND, typename R, int CT, int BLOCK>
 __host__ __device__ constexpr int min_blocks()
 {
@@ -211,10 +213,15 @@ __device__ __forceinline__ void face_means(MarchArgs<R, G> const & a, int64_t ic
 // integral over the cell's BCEs, divided by the CCE volume.
 //
 // With CACHE set (the fused march, where every record's primitive cache is
-// valid) a neighbour's primitives come from its record.
+// valid) a neighbour's primitives come from its record.  With u0 (the cell's
+// own current state; the FP32 march) the neighbour values enter as
+// differences from u0 and d0 receives so0n - u0: in FP32 the absolute
+// rounding then scales with the change, not with the state (the gradients
+// calc_dsoln forms from these differences are O(h) of the state).
 template <int CT, typename R, typename G, bool CACHE = false>
 __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n,
-                                          Carry<CellT<CT>::ND, CellT<CT>::NFC, R> * carry = nullptr)
+                                          Carry<CellT<CT>::ND, CellT<CT>::NFC, R> * carry = nullptr,
+                                          R const * u0 = nullptr, R * d0 = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -263,7 +270,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
 #pragma unroll
             for (int i = 0; i < NEQ; ++i)
             {
-                R pp = u[i] + a.hdt * t[i];
+                R pp = (u0 ? u[i] - u0[i] : u[i]) + a.hdt * t[i];
                 R qq = R(0);
 #pragma unroll
                 for (int d = 0; d < ND; ++d)
@@ -279,7 +286,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
 #pragma unroll
         for (int i = 0; i < NEQ; ++i)
         {
-            R s = u[i];
+            R s = u0 ? u[i] - u0[i] : u[i];
 #pragma unroll
             for (int d = 0; d < ND; ++d)
             {
@@ -326,7 +333,17 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
 #pragma unroll
     for (int i = 0; i < NEQ; ++i)
     {
-        so0n[i] = acc[i].value() * ivol;
+        if (u0)
+        {
+            // Delta form: the CCE volume is the sum of the BCE volumes, so
+            // sum_f bvol_f u0 / cevol = u0 and only the change is summed.
+            d0[i] = acc[i].value() * ivol;
+            so0n[i] = u0[i] + d0[i];
+        }
+        else
+        {
+            so0n[i] = acc[i].value() * ivol;
+        }
     }
 }
 
@@ -380,7 +397,8 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 template <int CT, typename R, typename G>
 __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
                                            R * so1n,
-                                           Carry<CellT<CT>::ND, CellT<CT>::NFC, R> const * carry = nullptr)
+                                           Carry<CellT<CT>::ND, CellT<CT>::NFC, R> const * carry = nullptr,
+                                           R const * u0 = nullptr, R const * d0 = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
     constexpr int NEQ = ND + 2;
@@ -486,7 +504,9 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
             for (int i = 0; i < NEQ; ++i)
             {
-                uf[f][i] = (carry->p[f][i] + tau * carry->q[f][i]) - so0n[i];
+                // carry->p already has the cell's own change (d0) or new state
+                // taken out (see fused_cell).
+                uf[f][i] = carry->p[f][i] + tau * carry->q[f][i];
             }
         }
     }
@@ -515,7 +535,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
             for (int i = 0; i < NEQ; ++i)
             {
-                R s = rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
+                R s = u0 ? (rec[i] - u0[i]) + a.hdt * rec[NEQ + i] - d0[i] : rec[i] + a.hdt * rec[NEQ + i] - so0n[i];
 #pragma unroll
                 for (int d = 0; d < ND; ++d)
                 {
@@ -880,8 +900,15 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     {
         face_means<CT, R, G>(a, icl, carry.mm, carry.mb);
     }
+    // FP32: work relative to the cell's own current state (delta form).
+    constexpr bool DELTA = sizeof(R) == 4;
+    R u0[NEQ], d0[NEQ];
+    if constexpr (DELTA)
+    {
+        load_rec<ND, R, NEQ>(a.cur + row * Rec<ND, R>::RS, u0);
+    }
     R so0n[NEQ];
-    soln_cell<CT, R, G, true>(a, icl, so0n, CARRY ? &carry : nullptr);
+    soln_cell<CT, R, G, true>(a, icl, so0n, CARRY ? &carry : nullptr, DELTA ? u0 : nullptr, d0);
 
     // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
 #pragma unroll
@@ -906,9 +933,28 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     }
 
     R rinv;
+    R const e_soln = so0n[NEQ - 1];
     R const cflc = cfl_cell<ND, R, G>(a, icl, row, so0n, rinv);
+    if (DELTA && so0n[NEQ - 1] != e_soln)
+    {
+        d0[NEQ - 1] = so0n[NEQ - 1] - u0[NEQ - 1]; // calc_cfl rewrote the energy
+    }
+    if constexpr (CARRY)
+    {
+        // Take the cell's own change (FP32, delta form) or new state out of
+        // the carried sums now, so it need not stay live through calc_dsoln.
+#pragma unroll
+        for (int f = 0; f < NFC; ++f)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                carry.p[f][i] -= DELTA ? d0[i] : so0n[i];
+            }
+        }
+    }
     R so1n[NEQ * ND];
-    dsoln_cell<CT, R, G>(a, icl, so0n, cflc, so1n, CARRY ? &carry : nullptr);
+    dsoln_cell<CT, R, G>(a, icl, so0n, cflc, so1n, CARRY ? &carry : nullptr, DELTA ? u0 : nullptr, d0);
     R so0t[NEQ];
     Prim<ND, R> const q(so0n, ldg(a.gamma + row), rinv);
     solt_prim<ND, R>(q, so0n, so1n, so0t);
