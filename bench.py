@@ -749,7 +749,7 @@ def run_serve(args, world, rank, dist):
     from solvcon_gb300 import serving
     nreq = args.nreq
     data = batch_meshes(args.nmesh, seed=4242 + 1000 * rank)
-    srv = serving.Server(hbm_budget=120 * 2 ** 30, max_chunk=64,
+    srv = serving.Server(hbm_budget=120 * 2 ** 30, max_chunk=args.max_chunk,
                          precision=args.precision or "fp32")
     for k, (m, s, f, g) in enumerate(data):
         srv.add_mesh(k, m, s, f, g, dt_for_cfl_g(m, s, 0.8, g))
@@ -787,7 +787,8 @@ def run_serve(args, world, rank, dist):
                                "tubes of 1k-100k points, 70%% 2D meshes of "
                                "the batched distribution, 200-2000 steps; "
                                "HBM budget 120 GB; continuous batching)"
-                               % nreq, "rates": rates},
+                               % nreq, "rates": rates,
+                   "max_chunk": args.max_chunk},
         "per_rate": per_rate,
         "baseline_alone_plain_fp64": {"value": alone_rate,
                                       "unit": "cell-steps/s",
@@ -1038,6 +1039,8 @@ def main():
     ap.add_argument("--nmesh", type=int, default=None)
     ap.add_argument("--nreq", type=int, default=64)
     ap.add_argument("--rates", default="50,200,1000,2000")
+    ap.add_argument("--max-chunk", type=int, default=32,
+                    help="serve: most steps one serving tick advances")
     args = ap.parse_args()
     if args.nmesh is None:
         args.nmesh = 512 if args.workload == "batch" else 64

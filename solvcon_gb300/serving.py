@@ -115,11 +115,13 @@ class Server:
 
     :param meshes: dict mesh_key -> _MeshSpec (see :meth:`add_mesh`).
     :param hbm_budget: device bytes the resident solvers may hold.
-    :param max_chunk: most steps one tick advances.
+    :param max_chunk: most steps one tick advances (measured on the mixed
+        workload of 1D tubes and 2D meshes: 32 gave 3.68 G cell-steps/s
+        aggregate, 16 gave 3.28, 64 3.46, 128 3.30, 256 3.12).
     :param precision: precision of the 2D solves.
     """
 
-    def __init__(self, hbm_budget=120 * 2 ** 30, max_chunk=64,
+    def __init__(self, hbm_budget=120 * 2 ** 30, max_chunk=32,
                  precision="fp32", block=64, persistent=True):
         self.meshes = {}
         self.hbm_budget = int(hbm_budget)
