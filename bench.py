@@ -765,6 +765,10 @@ def run_serve(args, world, rank, dist):
         st["rate_req_per_s"] = rate
         st["rejected"] = len(srv.rejected)
         st["peak_resident"] = srv.peak_resident
+        st["ticks"] = srv.ticks
+        st["batch_rebuilds"] = srv.rebuilds
+        st["seconds_rebuild_march_tubes"] = [srv.t_rebuild, srv.t_batch,
+                                             srv.t_tubes]
         per_rate.append(st)
     # Each request alone with the plain FP64 march (the same request set).
     reqs = serving.make_requests(nreq, 1.0, keys, seed=7)

@@ -302,6 +302,12 @@ typedef struct scg_batch scg_batch;
  * resident capacity (blocks stride over tiles) instead of one block per tile. */
 int scg_batch_create(scg_euler * const * cores, int64_t ncore, int block, int persistent, scg_batch ** out);
 int scg_batch_destroy(scg_batch * batch);
+/* Point an existing batch at another set of cores (its stream, device tables
+ * and occupancy are kept; the step graph is captured again at the next
+ * march).  *done = 0, and nothing changes, when the new set needs another
+ * kernel (other ndim, precision, or cell-type specialisation): create a new
+ * batch then. */
+int scg_batch_retarget(scg_batch * batch, scg_euler * const * cores, int64_t ncore, int * done);
 /* out[5] = ncore, total body cells, tiles, grid, block. */
 int scg_batch_info(const scg_batch * batch, int64_t * out);
 /* march(steps) of every core; synchronous. */

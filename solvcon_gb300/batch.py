@@ -29,6 +29,7 @@ lib = _lib.bind_more({
     "scg_batch_create": ([_vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                           _vp], ctypes.c_int),
     "scg_batch_destroy": ([_vp], ctypes.c_int),
+    "scg_batch_retarget": ([_vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
     "scg_batch_info": ([_vp, _vp], ctypes.c_int),
     "scg_batch_march": ([_vp, ctypes.c_int64], ctypes.c_int),
     "scg_batch_last_ms": ([_vp, _vp], ctypes.c_int),
@@ -64,6 +65,25 @@ class EulerBatch:
         if h is not None and h.value:
             lib.scg_batch_destroy(h)
             self._h = None
+
+    def retarget(self, cores):
+        """March another set of cores with this batch (its stream, device
+        tables and occupancy kept; the step graph is captured again).
+        Returns False, changing nothing, when the set needs another kernel
+        (other ndim or precision, or another cell-type specialisation)."""
+        cores = list(cores)
+        arr = (ctypes.c_void_p * len(cores))(*[c.handle.value for c in cores])
+        done = ctypes.c_int()
+        check(lib.scg_batch_retarget(self._h, arr, len(cores),
+                                     ctypes.byref(done)))
+        if not done.value:
+            return False
+        self.cores = cores
+        info = np.zeros(5, dtype="int64")
+        check(lib.scg_batch_info(self._h, ptr(info)))
+        self.ncore, self.ncell, self.ntiles, self.grid, self.block = \
+            (int(x) for x in info)
+        return True
 
     def march(self, steps):
         """Advance every core ``steps`` full steps (synchronous)."""

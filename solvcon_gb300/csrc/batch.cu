@@ -101,6 +101,10 @@ constexpr auto batch_kernel()
 struct BatchBase
 {
     virtual ~BatchBase() = default;
+    // Point the batch at another set of cores, keeping its stream, device
+    // tables (grown when too small) and occupancy; false (and nothing
+    // changed) when the set needs another kernel than this batch's.
+    virtual bool retarget(std::vector<scg::EulerCoreBase *> cores) = 0;
     virtual void march(int64_t steps) = 0;
     virtual void sync() = 0;
     virtual cudaStream_t get_stream() const = 0;
@@ -116,13 +120,109 @@ public:
     using Args = MarchArgs<R, G>;
 
     Batch(std::vector<scg::EulerCoreBase *> cores_in, bool persistent)
-        : cores(std::move(cores_in))
+        : cores(std::move(cores_in)), persistent(persistent)
     {
         block = B;
-        ncore = static_cast<int64_t>(cores.size());
         scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         scg::cuda_check(cudaEventCreate(&ev[0]), "event");
         scg::cuda_check(cudaEventCreate(&ev[1]), "event");
+        int dev = 0, nsm = 0, occ = 0;
+        scg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        scg::cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
+        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<ND, R, G, B, CT1>(), B, 0),
+                        "occupancy");
+        resident = static_cast<int64_t>(nsm) * std::max(occ, 1);
+        layout();
+    }
+
+    // The precision code of the cores this instantiation marches.
+    static constexpr int PREC = sizeof(R) == 8 ? scg::PREC_FP64
+                                               : (sizeof(G) == 8 ? scg::PREC_FP32_GEOM64 : scg::PREC_FP32);
+
+    bool retarget(std::vector<scg::EulerCoreBase *> cs) override
+    {
+        if (cs.empty())
+        {
+            throw std::invalid_argument("EulerBatch: no cores");
+        }
+        constexpr int SIMPLEX = (ND == 2) ? scg::CT_TRIANGLE : scg::CT_TET;
+        bool all = true;
+        for (auto * c : cs)
+        {
+            if (c->ndim != ND || c->precision != PREC)
+            {
+                return false;
+            }
+            all = all && c->single_ct == SIMPLEX;
+        }
+        // make_for_block's choice for the new set must be this kernel.
+        if ((CT1 != 0) != all)
+        {
+            return false;
+        }
+        sync();
+        cores = std::move(cs);
+        Args const * const d0 = descs[0].ptr;
+        Args const * const d1 = descs[1].ptr;
+        int2 const * const t0 = tiles.ptr;
+        layout();
+        if (graph_exec && (descs[0].ptr != d0 || descs[1].ptr != d1 || tiles.ptr != t0 || !update_graph()))
+        {
+            drop_graph(); // captured again at the next march
+        }
+        return true;
+    }
+
+    // Point the captured step's two kernel nodes at the new work list (its
+    // length and the grid; the device tables did not move) without capturing
+    // again.  False when the runtime refuses the update.
+    bool update_graph()
+    {
+        for (cudaGraphNode_t node : graph_nodes)
+        {
+            cudaKernelNodeParams p{};
+            if (cudaGraphKernelNodeGetParams(node, &p) != cudaSuccess || !p.kernelParams)
+            {
+                (void)cudaGetLastError();
+                return false;
+            }
+            Args const * d = *static_cast<Args const * const *>(p.kernelParams[0]);
+            int2 const * t = tiles.ptr;
+            int n = static_cast<int>(ntiles);
+            void * args[3] = {&d, &t, &n};
+            p.gridDim = dim3(static_cast<unsigned>(grid), 1, 1);
+            p.kernelParams = args;
+            p.extra = nullptr;
+            if (cudaGraphExecKernelNodeSetParams(graph_exec, node, &p) != cudaSuccess)
+            {
+                (void)cudaGetLastError();
+                return false;
+            }
+        }
+        return true;
+    }
+
+    void drop_graph()
+    {
+        if (graph_exec)
+        {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        if (graph)
+        {
+            cudaGraphDestroy(graph);
+            graph = nullptr;
+        }
+        graph_nodes.clear();
+    }
+
+    // The work list of (core, row tile) pairs, the device tables sized for
+    // it (grown, never shrunk) and the grid.
+    void layout()
+    {
+        ncore = static_cast<int64_t>(cores.size());
+        ncell = 0;
         std::vector<int2> tl;
         for (int64_t c = 0; c < ncore; ++c)
         {
@@ -143,21 +243,22 @@ public:
         {
             throw std::invalid_argument("EulerBatch: work list too long");
         }
-        tiles.alloc(std::max<size_t>(tl.size(), 1));
+        if (tiles.n < tl.size() || !tiles.ptr)
+        {
+            tiles.alloc(std::max<size_t>(tl.size() + tl.size() / 2, 1));
+        }
         if (!tl.empty())
         {
             scg::cuda_check(cudaMemcpy(tiles.ptr, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice), "H2D");
         }
+        size_t const nd = static_cast<size_t>(std::max<int64_t>(ncore, 1));
         for (auto & d : descs)
         {
-            d.alloc(static_cast<size_t>(std::max<int64_t>(ncore, 1)));
+            if (d.n < nd || !d.ptr)
+            {
+                d.alloc(nd + nd / 2);
+            }
         }
-        int dev = 0, nsm = 0, occ = 0;
-        scg::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-        scg::cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "attr");
-        scg::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<ND, R, G, B, CT1>(), B, 0),
-                        "occupancy");
-        int64_t const resident = static_cast<int64_t>(nsm) * std::max(occ, 1);
         grid = persistent ? std::min<int64_t>(ntiles, resident) : ntiles;
         grid = std::max<int64_t>(grid, 1);
     }
@@ -166,8 +267,7 @@ public:
     {
         cudaEventDestroy(ev[0]);
         cudaEventDestroy(ev[1]);
-        if (graph_exec)
-            cudaGraphExecDestroy(graph_exec);
+        drop_graph();
         if (stream)
         {
             cudaStreamSynchronize(stream);
@@ -212,16 +312,20 @@ public:
         }
     }
 
+    // The step's two launches as a graph; the graph and its kernel nodes are
+    // kept for update_graph.
     void capture()
     {
-        cudaGraph_t g = nullptr;
         scg::cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "BeginCapture");
         int64_t const before = scg::g_launches.load();
         launch_step();
         scg::g_launches.store(before);
-        scg::cuda_check(cudaStreamEndCapture(stream, &g), "EndCapture");
-        scg::cuda_check(cudaGraphInstantiate(&graph_exec, g, 0), "GraphInstantiate");
-        cudaGraphDestroy(g);
+        scg::cuda_check(cudaStreamEndCapture(stream, &graph), "EndCapture");
+        scg::cuda_check(cudaGraphInstantiate(&graph_exec, graph, 0), "GraphInstantiate");
+        size_t n = 0;
+        scg::cuda_check(cudaGraphGetNodes(graph, nullptr, &n), "GraphGetNodes");
+        graph_nodes.resize(n);
+        scg::cuda_check(cudaGraphGetNodes(graph, graph_nodes.data(), &n), "GraphGetNodes");
     }
 
     void march(int64_t steps) override
@@ -257,9 +361,13 @@ public:
 
 private:
     std::vector<scg::EulerCoreBase *> cores;
+    bool persistent = true;
+    int64_t resident = 1; // SM count x resident blocks of this kernel
     scg::DevBuf<Args> descs[2];
     scg::DevBuf<int2> tiles;
     cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    std::vector<cudaGraphNode_t> graph_nodes;
     cudaGraphExec_t graph_exec = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
 };
@@ -349,6 +457,26 @@ int scg_batch_create(scg_euler * const * cores, int64_t ncore, int block, int pe
         auto h = std::make_unique<scg_batch>();
         h->b = make_batch(std::move(v), block, persistent != 0);
         *out = h.release();
+    });
+}
+
+int scg_batch_retarget(scg_batch * batch, scg_euler * const * cores, int64_t ncore, int * done)
+{
+    return scg::guarded([&] {
+        if (!batch || !done)
+        {
+            throw std::invalid_argument("scg_batch_retarget: null argument");
+        }
+        std::vector<scg::EulerCoreBase *> v;
+        for (int64_t i = 0; i < ncore; ++i)
+        {
+            if (!cores[i] || !cores[i]->c)
+            {
+                throw std::invalid_argument("EulerBatch: null core handle");
+            }
+            v.push_back(cores[i]->c.get());
+        }
+        *done = batch->b->retarget(std::move(v)) ? 1 : 0;
     });
 }
 

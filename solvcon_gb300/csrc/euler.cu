@@ -805,7 +805,11 @@ public:
         stream = s ? s : own_stream;
     }
 
-    void sync() override { cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+    void sync() override
+    {
+        cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+        async_pending = false;
+    }
 
     cudaStream_t get_stream() const override { return stream; }
 
@@ -1320,6 +1324,7 @@ public:
             march_substep();
             march_substep();
         }
+        async_pending = steps > 0 && nrow > 0;
     }
 
     void limiter_mask(uint8_t * out) override
@@ -1385,8 +1390,12 @@ public:
             launched(stream, "calc_solt");
             next_valid = true;
             next_buf = cur ^ 1;
+            sync();
         }
-        sync();
+        else if (async_pending || stream != own_stream)
+        {
+            sync(); // a march of this core, or a caller's stream, may still run
+        }
     }
 
     void fill_args(int offset, void * out, size_t size) override
@@ -1514,6 +1523,7 @@ private:
     int cur = 0;           // index of the current (so0c/so1c) record buffer
     int tbuf = 0;          // buffer holding the logical so0t
     bool next_valid = false; // rec[next_buf].so0t (and its primitive cache) == calc_solt of rec[next_buf]
+    bool async_pending = false; // march() returned with its kernels possibly still running
     int next_buf = 1;
 };
 

@@ -132,6 +132,12 @@ class Server:
         self.slots = collections.defaultdict(list)
         self.held = 0
         self.ticks = 0
+        # Where a run's wall time went: building batches (a resident set
+        # that changed), marching them, and waiting for the 1D tubes.
+        self.rebuilds = 0
+        self.t_rebuild = 0.0
+        self.t_batch = 0.0
+        self.t_tubes = 0.0
         self.peak_resident = 0
         self.peak_held = 0
         self.rejected = []
@@ -222,6 +228,8 @@ class Server:
         """Serve ``requests`` (arrival times in seconds from the start);
         returns the list of finished requests."""
         pending = sorted(requests, key=lambda r: r.arrival)
+        self.ticks = self.rebuilds = 0
+        self.t_rebuild = self.t_batch = self.t_tubes = 0.0
         queue = collections.deque()
         active = {}
         finished = []
@@ -271,14 +279,22 @@ class Server:
             if meshes:
                 members = tuple(sorted(r.rid for r, _ in meshes))
                 if batch is None or members != batch_members:
-                    batch = EulerBatch([s.solver for _, s in meshes],
-                                       block=self.block,
-                                       persistent=self.persistent)
+                    tb = clock()
+                    solvers = [s.solver for _, s in meshes]
+                    if batch is None or not batch.retarget(solvers):
+                        batch = EulerBatch(solvers, block=self.block,
+                                           persistent=self.persistent)
                     batch_members = members
+                    self.rebuilds += 1
+                    self.t_rebuild += clock() - tb
+                tb = clock()
                 batch.march(chunk)
+                self.t_batch += clock() - tb
+            tb = clock()
             for r, s in tubes:
                 check(lib1d.scg_e1d_sync(s.solver.handle))
                 s.solver._after()
+            self.t_tubes += clock() - tb
             self.ticks += 1
             for rid in list(active):
                 r, s = active[rid]

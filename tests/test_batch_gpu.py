@@ -133,3 +133,28 @@ def test_batch_rejects_mixed_cores():
         EulerBatch([a[0][1], b[0][1]])
     with pytest.raises(ValueError):
         EulerBatch([a[0][1]], block=100)
+
+
+def test_retarget_keeps_results_exact():
+    """A batch pointed at another set of cores marches them exactly as
+    marching each alone; a set that needs another kernel is refused."""
+    from solvcon_gb300.batch import EulerBatch
+    seeds = [3, 11, 17, 29]
+    alone = _cores(2, "fp32", seeds)
+    together = _cores(2, "fp32", seeds)
+    for _, c in alone[:3]:
+        c.march(2)
+    for _, c in alone[1:]:
+        c.march(3)
+    b = EulerBatch([c for _, c in together[:3]], block=64)
+    b.march(2)
+    assert b.retarget([c for _, c in together[1:]])
+    assert b.ncore == 3
+    assert b.ncell == sum(c.ncell for _, c in together[1:])
+    b.march(3)
+    for (_, a), (_, t) in zip(alone, together):
+        np.testing.assert_array_equal(t.so0n.ndarray, a.so0n.ndarray)
+        np.testing.assert_array_equal(t.so1n.ndarray, a.so1n.ndarray)
+    other = _cores(2, "fp64", [5])
+    assert not b.retarget([other[0][1]])
+    assert b.ncore == 3
