@@ -79,7 +79,8 @@ def build(verbose=False, extra=()):
     lib = os.path.join(OUTDIR, LIBNAME)
     if not os.path.exists(lib) or \
             os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc(), ARCH, "-shared", "-o", lib] + objs + ["-lcudart"]
+        cmd = [nvcc(), ARCH, "-shared", "-o", lib] + objs + ["-lcudart",
+                                                            "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" %

@@ -697,8 +697,8 @@ public:
         nrow = ncell + ngstcell;
         m_nface = mesh.nface;
         m_ngstface = mesh.ngstface;
-        m_fccls = mesh.fccls.buf;
-        m_fcnml = mesh.fcnml.buf;
+        m_fccls.assign(mesh.fccls.buf.begin(), mesh.fccls.buf.end());
+        m_fcnml.assign(mesh.fcnml.buf.begin(), mesh.fcnml.buf.end());
         m_stm.assign(static_cast<size_t>(nrow * NEQ), 0.0);
         cuda_check(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         stream = own_stream;
@@ -1480,8 +1480,8 @@ private:
         return m_staging.ptr;
     }
 
-    template <typename T>
-    void up(DevBuf<T> & d, std::vector<T> const & h)
+    template <typename T, typename A>
+    void up(DevBuf<T> & d, std::vector<T, A> const & h)
     {
         d.alloc(std::max<size_t>(h.size(), 1));
         if (!h.empty())

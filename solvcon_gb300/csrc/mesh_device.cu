@@ -519,13 +519,23 @@ void HostMesh::build_interior_device(bool do_metric, bool do_edge)
     k_clfcs<<<grid_of(ncell), TB>>>(raw(tclfcs), raw(map2), ncell, raw(d_clfcs));
     cuda_check(cudaGetLastError(), "k_clfcs");
 
-    remake(fctpn, 0, nface, 1, -1);
-    remake(fcnds, 0, nface, FCMND + 1, -1);
-    remake(fccls, 0, nface, FCREL, -1);
-    remake(fccnd, 0, nface, ndim, 0.0);
-    remake(fcnml, 0, nface, ndim, 0.0);
-    remake(fcara, 0, nface, 1, 0.0);
-    remake(clfcs, 0, ncell, CLMFC + 1, -1);
+    // Tables the device results overwrite in full are not filled first.
+    remake_unset(fctpn, 0, nface, 1);
+    remake_unset(fcnds, 0, nface, FCMND + 1);
+    remake_unset(fccls, 0, nface, FCREL);
+    remake_unset(clfcs, 0, ncell, CLMFC + 1);
+    if (do_metric)
+    {
+        remake_unset(fccnd, 0, nface, ndim);
+        remake_unset(fcnml, 0, nface, ndim);
+        remake_unset(fcara, 0, nface, 1);
+    }
+    else
+    {
+        remake(fccnd, 0, nface, ndim, 0.0);
+        remake(fcnml, 0, nface, ndim, 0.0);
+        remake(fcara, 0, nface, 1, 0.0);
+    }
     if (do_metric)
     {
         device_vector<double> d_ndcrd(ndcrd.buf.begin(), ndcrd.buf.end());

@@ -14,6 +14,7 @@
 #include <numeric>
 #include <set>
 #include <stdexcept>
+#include <thread>
 #include <type_traits>
 #include <utility>
 
@@ -625,17 +626,63 @@ void HostMesh::remake(Table<T> & t, int64_t ngst, int64_t nb, int64_t w, T init)
     t.make(ngst, nb, w, init);
 }
 
+template <typename T>
+void HostMesh::remake_unset(Table<T> & t, int64_t ngst, int64_t nb, int64_t w)
+{
+    if constexpr (std::is_same_v<T, double>)
+        m_retired_real.push_back(std::move(t.buf));
+    else
+        m_retired_int.push_back(std::move(t.buf));
+    t.make_unset(ngst, nb, w);
+}
+
 // Used by the device builder (mesh_device.cu) as well.
 template void HostMesh::remake<int32_t>(Table<int32_t> &, int64_t, int64_t, int64_t, int32_t);
 template void HostMesh::remake<double>(Table<double> &, int64_t, int64_t, int64_t, double);
+template void HostMesh::remake_unset<int32_t>(Table<int32_t> &, int64_t, int64_t, int64_t);
+template void HostMesh::remake_unset<double>(Table<double> &, int64_t, int64_t, int64_t);
 
 template <typename T>
 void HostMesh::regrow(Table<T> & t, int64_t ngst, T init)
 {
+    // The ghost rows go first: a new buffer, its ghost rows set to init and
+    // the body copied after them, by several threads (one pass over memory
+    // instead of a fill and a copy by one thread).
     Table<T> n;
-    n.make(ngst, t.nbody, t.width, init);
-    std::copy(t.buf.begin() + static_cast<std::ptrdiff_t>(t.nghost * t.width), t.buf.end(),
-              n.buf.begin() + static_cast<std::ptrdiff_t>(ngst * t.width));
+    n.nghost = ngst;
+    n.nbody = t.nbody;
+    n.width = t.width;
+    size_t const head = static_cast<size_t>(ngst * t.width);
+    size_t const body = static_cast<size_t>(t.nbody * t.width);
+    n.buf.resize(head + body);
+    T const * const src = t.buf.data() + static_cast<size_t>(t.nghost * t.width);
+    T * const dst = n.buf.data();
+    size_t const total = head + body;
+    size_t const nthr = std::max<size_t>(
+        1, std::min<size_t>(std::thread::hardware_concurrency(), std::min<size_t>(16, total / (1 << 20) + 1)));
+    auto work = [&](size_t k) {
+        size_t const lo = total * k / nthr;
+        size_t const hi = total * (k + 1) / nthr;
+        for (size_t i = lo; i < std::min(hi, head); ++i)
+        {
+            dst[i] = init;
+        }
+        size_t const b0 = std::max(lo, head);
+        if (hi > b0)
+        {
+            std::copy(src + (b0 - head), src + (hi - head), dst + b0);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nthr; ++k)
+    {
+        pool.emplace_back(work, k);
+    }
+    work(0);
+    for (auto & th : pool)
+    {
+        th.join();
+    }
     if constexpr (std::is_same_v<T, double>)
         m_retired_real.push_back(std::move(t.buf));
     else

@@ -15,7 +15,9 @@
  */
 
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace scg
@@ -54,10 +56,42 @@ struct BcGroup
     int64_t nbound() const { return static_cast<int64_t>(facn.size() / BFREL); }
 };
 
+// An allocator whose default construction leaves trivial elements
+// uninitialised, so a table can be sized without a first pass of zeros
+// (the tables of a 24.6M-cell mesh are ~7 GB; build_ghost re-lays all of
+// them out with ghost rows first).
+template <typename T>
+struct NoInit : std::allocator<T>
+{
+    template <typename U>
+    struct rebind
+    {
+        using other = NoInit<U>;
+    };
+    NoInit() = default;
+    template <typename U>
+    NoInit(NoInit<U> const &) noexcept
+    {
+    }
+    template <typename U>
+    void construct(U * p) noexcept
+    {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <typename U, typename... Args>
+    void construct(U * p, Args &&... args)
+    {
+        ::new (static_cast<void *>(p)) U(std::forward<Args>(args)...);
+    }
+};
+
+template <typename T>
+using HostVec = std::vector<T, NoInit<T>>;
+
 template <typename T>
 struct Table
 {
-    std::vector<T> buf;
+    HostVec<T> buf;
     int64_t nghost = 0;
     int64_t nbody = 0;
     int64_t width = 1; // product of the trailing extents
@@ -68,6 +102,15 @@ struct Table
         nbody = nb;
         width = w;
         buf.assign(static_cast<size_t>((ngst + nb) * w), init);
+    }
+    // The same shape with the contents left for the caller to write in full.
+    void make_unset(int64_t ngst, int64_t nb, int64_t w)
+    {
+        nghost = ngst;
+        nbody = nb;
+        width = w;
+        buf.clear();
+        buf.resize(static_cast<size_t>((ngst + nb) * w));
     }
     T & operator()(int64_t i, int64_t j = 0) { return buf[static_cast<size_t>((i + nghost) * width + j)]; }
     T const & operator()(int64_t i, int64_t j = 0) const { return buf[static_cast<size_t>((i + nghost) * width + j)]; }
@@ -113,8 +156,11 @@ private:
     void remake(Table<T> & t, int64_t ngst, int64_t nb, int64_t w, T init);
     template <typename T>
     void regrow(Table<T> & t, int64_t ngst, T init);
-    std::vector<std::vector<double>> m_retired_real;
-    std::vector<std::vector<int32_t>> m_retired_int;
+    // remake without the fill, for a table the caller overwrites entirely.
+    template <typename T>
+    void remake_unset(Table<T> & t, int64_t ngst, int64_t nb, int64_t w);
+    std::vector<HostVec<double>> m_retired_real;
+    std::vector<HostVec<int32_t>> m_retired_int;
 
     void validate_cells() const;
     void build_faces_from_cells();
