@@ -471,8 +471,8 @@ def test_march_matches_reference_golden():
 
 # -- FP32-state variants: error against the FP64 oracle -----------------------
 
-@pytest.mark.parametrize("ndim", [2, 3])
-def test_fp32_state_error_against_oracle(ndim):
+@pytest.mark.parametrize("kind", ["tri", "tet", "quad", "hex", "prism"])
+def test_fp32_state_error_against_oracle(kind):
     """FP32-state march (FP32 flux arithmetic with compensated face sums,
     FP64-computed geometry) against the FP64 oracle at the workloads' CFL.
 
@@ -482,14 +482,24 @@ def test_fp32_state_error_against_oracle(ndim):
     min/max switches (the FP64 march itself drifts from the oracle by ~1e-6
     relative L1 after a few hundred steps), so the bound is 2e-5 per variable
     and 1e-5 on the whole state.  Totals: FP64 totals of the FP32 march within
-    1e-6 relative of the oracle's for mass and energy."""
+    1e-6 relative of the oracle's for mass and energy.  Triangles and
+    tetrahedra run the kernels compiled for one simplex type (neighbour
+    terms carried); quadrilaterals, hexahedra and prisms the kernels that
+    dispatch on the cell type (neighbour records gathered twice)."""
     import bench
     from oracle import oracle as ora
     from solvcon_gb300 import meshgen
-    if ndim == 2:
+    ndim = 2 if kind in ("tri", "quad") else 3
+    if kind == "tri":
         x, t, c = meshgen.tri_square(48, 0.2, seed=31)
-    else:
+    elif kind == "quad":
+        x, t, c = meshgen.quad_square(48, 0.15, seed=31)
+    elif kind == "tet":
         x, t, c = meshgen.tet_cube(8, 0.15, seed=31)
+    elif kind == "hex":
+        x, t, c = meshgen.hex_cube(12, 0.1, seed=31)
+    else:
+        x, t, c = meshgen.prism_slab(12, 6, 0.1, seed=31)
     mesh = meshgen.build_mesh(ndim, x, t, c)
     ng = mesh.ngstcell
     clcnd = np.array(mesh.clcnd.ndarray)[ng:]
