@@ -13,7 +13,6 @@ import ctypes
 
 import numpy as np
 
-from . import _lib
 from ._lib import check, lib, ptr
 from .buffer import SimpleArray
 
@@ -196,7 +195,6 @@ def _make_prop(i):
 for _i, _name in enumerate(_ARRAYS):
     setattr(StaticMesh, _name, _make_prop(_i))
 del _i, _name, _make_prop
-_ = _lib
 
 
 class Gmsh:

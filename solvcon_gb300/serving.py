@@ -22,13 +22,10 @@ same precision (batched marches are per-core exact).
 """
 
 import collections
-import ctypes
-import heapq
 import time
 
 import numpy as np
 
-from . import meshgen
 from .batch import EulerBatch
 from .multidim import EulerCore
 from .onedim import Euler1DCore, lib as lib1d
@@ -370,5 +367,3 @@ def make_requests(n, rate, mesh_keys, seed=0, frac_1d=0.3, steps=(200, 2000)):
             out.append(Request(k, "2d", nsteps, arr[k], mesh_key=key))
     return out
 
-
-_ = (ctypes, heapq, meshgen)
