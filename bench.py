@@ -349,6 +349,18 @@ def cpu_nside(workload, steps):
     return int(max(4, min(40, round((cells / 6.0) ** (1.0 / 3.0)))))
 
 
+def pin_device(local):
+    """One GPU per rank: the local rank's device, as the only visible one
+    (the local-th entry when a device list is already set)."""
+    seen = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if seen is None:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        return
+    devs = [d for d in seen.split(",") if d.strip()]
+    if len(devs) > 1 and local < len(devs):
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local].strip()
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1056,7 +1068,7 @@ def main():
         return
     if args.workload in ("batch", "serve", "accuracy", "meshbuild") or (
             args.workload in LINE_WORKLOADS and args.impl != "reference"):
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        pin_device(local)
         import solvcon_gb300  # noqa: F401
         {"batch": run_batch, "serve": run_serve, "accuracy": run_accuracy,
          "meshbuild": run_meshbuild,
@@ -1068,7 +1080,7 @@ def main():
     precision = args.precision or ("fp64" if args.workload == "tri2d"
                                    else "fp32")
 
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    pin_device(local)
     import solvcon_gb300  # noqa: F401  (fails loudly without libscg.so)
     from solvcon_gb300._lib import check, lib
 

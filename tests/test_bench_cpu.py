@@ -75,3 +75,17 @@ def test_batch_mesh_morton_is_a_renumbering():
     assert not np.array_equal(perm, np.arange(ma.ncell))
     np.testing.assert_array_equal(b[1], a[1][perm])
     assert a[3] == b[3] and len(a[2]) == len(b[2])
+
+
+def test_pin_device_one_gpu_per_rank(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    bench.pin_device(3)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "3"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "4,5,6,7")
+    bench.pin_device(2)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "6"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "5")
+    bench.pin_device(0)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "5"
