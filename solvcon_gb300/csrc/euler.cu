@@ -725,6 +725,8 @@ public:
         mv.clfcs = d_clfcs.ptr;
         mv.cltpn = d_cltpn.ptr;
 
+        validate_connectivity(mesh.nface, mesh.nnode);
+
         nslot = 0;
         for (int64_t icl = 0; icl < ncell; ++icl)
         {
@@ -797,6 +799,31 @@ public:
         for (auto const & c : ce)
             b += c.bytes();
         return b;
+    }
+
+    // Every body cell's faces, their cells and nodes in range, and every face
+    // shared with the cell that lists it, so no kernel can index outside a
+    // table whatever a caller wrote into the mesh (checked on the device).
+    void validate_connectivity(int64_t nface, int64_t nnode)
+    {
+        if (ncell == 0)
+        {
+            return;
+        }
+        DevBuf<unsigned long long> bad(1);
+        unsigned long long const none = ~0ull;
+        cuda_check(cudaMemcpyAsync(bad.ptr, &none, sizeof(none), cudaMemcpyHostToDevice, stream), "H2D");
+        k_validate_mesh<<<grid_for(ncell), BLOCK, 0, stream>>>(mv, nface, nnode, bad.ptr);
+        launched(stream, "validate_mesh");
+        unsigned long long first = none;
+        cuda_check(cudaMemcpyAsync(&first, bad.ptr, sizeof(first), cudaMemcpyDeviceToHost, stream), "D2H");
+        sync();
+        if (first != none)
+        {
+            throw std::invalid_argument("EulerCore: mesh connectivity of cell " + std::to_string(first) +
+                                        " is inconsistent (a face, face cell or node out of range, or a face "
+                                        "that does not have the cell)");
+        }
     }
 
     void set_stream(cudaStream_t s) override
@@ -954,6 +981,11 @@ public:
                 {
                     throw std::runtime_error("EulerCore: boundary face " + std::to_string(ifc) +
                                              " has no ghost cell; build the ghost layer first");
+                }
+                if (icl < 0 || icl >= ncell)
+                {
+                    throw std::invalid_argument("EulerCore: boundary face " + std::to_string(ifc) +
+                                                " has no interior cell (fccls[0] = " + std::to_string(icl) + ")");
                 }
                 kind[g] = static_cast<int8_t>(b.kind);
                 gint[g] = static_cast<int32_t>(icl + ngstcell);

@@ -36,6 +36,47 @@ struct MeshView
     __device__ int32_t rcl(int32_t ifc, int32_t icl) const { return fcls(ifc, 0) + fcls(ifc, 1) - icl; }
 };
 
+// Range check of what the set-up and march kernels index through: for body
+// cell icl, its face count and faces, each face's two cells (one of them icl)
+// and its node count and nodes.  Reads only inside the tables; the first bad
+// cell lands in *bad (atomicMin).
+__global__ void k_validate_mesh(MeshView m, int64_t nface, int64_t nnode, unsigned long long * bad)
+{
+    int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (icl >= m.ncell)
+    {
+        return;
+    }
+    bool ok = true;
+    int const nf = m.cfcs(icl, 0);
+    ok = nf >= 1 && nf <= 6;
+    for (int k = 1; ok && k <= nf; ++k)
+    {
+        int64_t const ifc = m.cfcs(icl, k);
+        if (ifc < -m.ngstface || ifc >= nface)
+        {
+            ok = false;
+            break;
+        }
+        int64_t const c0 = m.fcls(ifc, 0);
+        int64_t const c1 = m.fcls(ifc, 1);
+        bool const mine = c0 == icl || c1 == icl;
+        int64_t const other = c0 == icl ? c1 : c0;
+        ok = mine && other >= -m.ngstcell && other < m.ncell;
+        int const nn = m.fnds(ifc, 0);
+        ok = ok && nn >= 1 && nn <= 4;
+        for (int j = 1; ok && j <= nn; ++j)
+        {
+            int64_t const ind = m.fnds(ifc, j);
+            ok = ind >= -m.ngstnode && ind < nnode;
+        }
+    }
+    if (!ok)
+    {
+        atomicMin(bad, static_cast<unsigned long long>(icl));
+    }
+}
+
 // Reference-layout CE geometry (FP64): cevol [nrowc][7], cecnd [nrowc][7*nd],
 // sfcnd/sfnml [ncell][24][nd].  Ghost rows of cevol/cecnd stay zero.
 struct CeView

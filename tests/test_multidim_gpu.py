@@ -531,3 +531,28 @@ def test_fp32_state_error_against_oracle(kind):
         tgot = ec.totals()
         for k in (0, ndim + 1):
             assert abs(tgot[k] - twant[k]) <= 1e-6 * abs(twant[k]), (prec, k)
+
+
+# -- connectivity written by a caller is checked before any kernel uses it ---
+
+@pytest.mark.parametrize("what", ["face", "face_cell", "node", "count"])
+def test_core_rejects_inconsistent_connectivity(what):
+    import solvcon_gb300 as sg
+    mesh = fixture_mesh("mixed")
+    ng, ngf = int(mesh.ngstcell), int(mesh.ngstface)
+    clfcs = mesh.clfcs.ndarray
+    fccls = mesh.fccls.ndarray
+    fcnds = mesh.fcnds.ndarray
+    ifc = int(clfcs[ng + 1, 1])
+    if what == "face":
+        clfcs[ng + 1, 1] = mesh.nface + 7
+    elif what == "face_cell":
+        # The face no longer lists cell 1 among its two cells.
+        fccls[ngf + ifc, 0] = 0 if fccls[ngf + ifc, 0] != 0 else 2
+        fccls[ngf + ifc, 1] = 0 if fccls[ngf + ifc, 1] != 0 else 2
+    elif what == "node":
+        fcnds[ngf + ifc, 1] = mesh.nnode + 3
+    else:
+        clfcs[ng + 1, 0] = 9
+    with pytest.raises(ValueError, match="connectivity of cell"):
+        sg.EulerCore(mesh=mesh, time_increment=0.01)
