@@ -779,8 +779,9 @@ def run_serve(args, world, rank, dist):
         st["peak_resident"] = srv.peak_resident
         st["ticks"] = srv.ticks
         st["batch_rebuilds"] = srv.rebuilds
-        st["seconds_rebuild_march_tubes"] = [srv.t_rebuild, srv.t_batch,
-                                             srv.t_tubes]
+        st["seconds_rebuild_march_tubes_load_result"] = [
+            srv.t_rebuild, srv.t_batch, srv.t_tubes, srv.t_load,
+            srv.t_result]
         per_rate.append(st)
     # Each request alone with the plain FP64 march (the same request set).
     reqs = serving.make_requests(nreq, 1.0, keys, seed=7)

@@ -151,6 +151,9 @@ int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
 #define SCG_OP_CALC_DSOLN 6
 #define SCG_OP_BC_DSOLN 7
 #define SCG_OP_MARCH_SUBSTEP 8
+/* Not a reference operation: the solution state back to that of a new core
+ * (the mesh, geometry and boundary conditions kept), for reusing a core. */
+#define SCG_OP_RESET_STATE 9
 
 /* Boundary kinds (euler.hpp:26-31). */
 #define SCG_BC_NONREFL 0

@@ -1284,6 +1284,21 @@ public:
         case EO_MARCH_SUBSTEP:
             march_substep();
             break;
+        case EO_RESET_STATE:
+            for (auto & r : rec)
+            {
+                cuda_check(cudaMemsetAsync(r.ptr, 0, r.bytes(), stream), "memset");
+            }
+            cuda_check(cudaMemsetAsync(d_gamma.ptr, 0, d_gamma.bytes(), stream), "memset");
+            cuda_check(cudaMemsetAsync(d_cflo.ptr, 0, d_cflo.bytes(), stream), "memset");
+            cuda_check(cudaMemsetAsync(d_cflc.ptr, 0, d_cflc.bytes(), stream), "memset");
+            cuda_check(cudaMemsetAsync(d_limiter.ptr, 0, d_limiter.bytes(), stream), "memset");
+            std::fill(m_stm.begin(), m_stm.end(), 0.0);
+            cur = 0;
+            tbuf = 0;
+            next_valid = false;
+            next_buf = 1;
+            break;
         default:
             throw std::invalid_argument("EulerCore: unknown operation " + std::to_string(which));
         }

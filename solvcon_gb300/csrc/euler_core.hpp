@@ -48,6 +48,10 @@ enum EulerOp : int
     EO_CALC_DSOLN = 6,
     EO_BC_DSOLN = 7,
     EO_MARCH_SUBSTEP = 8,
+    // Not a reference operation: the solution state back to that of a new
+    // core (records, CFL numbers, gamma, limiter mask and stm zero; buffer
+    // bookkeeping reset), the mesh, geometry and boundary conditions kept.
+    EO_RESET_STATE = 9,
 };
 
 enum EulerBCKind : int

@@ -32,7 +32,7 @@ ARRAYS = ("cevol", "cecnd", "sfcnd", "sfnml", "so0c", "so0n", "so0t", "so1c",
 _ID = {n: i for i, n in enumerate(ARRAYS)}
 _OPS = {"prepare_ce": 0, "update": 1, "calc_solt": 2, "calc_soln": 3,
         "bc_soln": 4, "calc_cfl": 5, "calc_dsoln": 6, "bc_dsoln": 7,
-        "march_substep": 8}
+        "march_substep": 8, "reset_state": 9}
 PRECISIONS = {"fp64": 0, "fp32-geom64": 1, "fp32": 2}
 _SWAP = (("so0c", "so0n"), ("so1c", "so1n"))
 
@@ -201,6 +201,13 @@ class EulerCore:
 
     def update(self):
         self._op("update", nswap=1)
+
+    def reset_state(self):
+        """Not in the reference: put the solution state back to that of a
+        new core (all solution arrays, CFL numbers and gamma zero), keeping
+        the mesh, the CE geometry and the boundary conditions, so a core can
+        be reused for another solve on the same mesh."""
+        self._op("reset_state")
 
     def calc_solt(self):
         self._op("calc_solt")

@@ -135,6 +135,8 @@ class Server:
         self.t_rebuild = 0.0
         self.t_batch = 0.0
         self.t_tubes = 0.0
+        self.t_load = 0.0
+        self.t_result = 0.0
         self.peak_resident = 0
         self.peak_held = 0
         self.rejected = []
@@ -193,9 +195,7 @@ class Server:
             core = slot.solver
             # A reused slot starts from the same all-zero tables as a new
             # solver, so the result does not depend on the slot's history.
-            for name in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo",
-                         "cflc"):
-                getattr(core, name)[...] = 0.0
+            core.reset_state()
             core.init_solution(spec.gamma, 1.0, [0.0] * spec.mesh.ndim, 1.0)
             core.so0n[0:] = spec.state
             core.bc_soln()
@@ -227,6 +227,7 @@ class Server:
         pending = sorted(requests, key=lambda r: r.arrival)
         self.ticks = self.rebuilds = 0
         self.t_rebuild = self.t_batch = self.t_tubes = 0.0
+        self.t_load = self.t_result = 0.0
         queue = collections.deque()
         active = {}
         finished = []
@@ -253,7 +254,9 @@ class Server:
                     break
                 queue.popleft()
                 slot.busy = True
+                tl = clock()
                 self._load(slot, req)
+                self.t_load += clock() - tl
                 req.t_admit = clock() - t0
                 active[req.rid] = (req, slot)
             if not active:
@@ -297,7 +300,9 @@ class Server:
                 r, s = active[rid]
                 r.done += chunk
                 if r.done >= r.steps:
+                    tl = clock()
                     r.result = self._result(s, r)
+                    self.t_result += clock() - tl
                     r.t_done = clock() - t0
                     s.busy = False
                     del active[rid]
