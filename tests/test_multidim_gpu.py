@@ -556,3 +556,39 @@ def test_core_rejects_inconsistent_connectivity(what):
         clfcs[ng + 1, 0] = 9
     with pytest.raises(ValueError, match="connectivity of cell"):
         sg.EulerCore(mesh=mesh, time_increment=0.01)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_reset_state_gives_a_fresh_core(precision):
+    """reset_state (not in the reference) puts a used core back to a new
+    core's state: the same march from the same start gives the same bits."""
+    from solvcon_gb300 import meshgen
+    x, t, c = meshgen.tri_square(12, 0.2, seed=9)
+    mesh = meshgen.build_mesh(2, x, t, c)
+    clcnd = np.array(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    state = meshgen.quadrant_state(clcnd, seed=9)
+    faces = [int(f) for f in mesh.bndfcs.ndarray[:, 0]]
+
+    def start(core):
+        core.init_solution(GAMMA, 1.0, [0.0, 0.0], 1.0)
+        core.so0n[0:] = state
+        core.bc_soln()
+        core.bc_dsoln()
+
+    used = _core(mesh, 2e-3, precision)
+    used.add_slipwall(faces)
+    start(used)
+    used.march(3)
+    used.update()  # leave the buffer bookkeeping off its initial state
+    used.reset_state()
+    for name in ("so0c", "so0n", "so1n", "cflo", "gamma"):
+        assert not np.array(getattr(used, name).ndarray).any(), name
+    start(used)
+    used.march(2)
+    fresh = _core(mesh, 2e-3, precision)
+    fresh.add_slipwall(faces)
+    start(fresh)
+    fresh.march(2)
+    for name in ("so0c", "so0n", "so0t", "so1c", "so1n", "cflo", "cflc"):
+        np.testing.assert_array_equal(getattr(used, name).ndarray,
+                                      getattr(fresh, name).ndarray, name)
