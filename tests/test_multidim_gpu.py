@@ -582,7 +582,7 @@ def test_reset_state_gives_a_fresh_core(precision):
     used.update()  # leave the buffer bookkeeping off its initial state
     used.reset_state()
     for name in ("so0c", "so0n", "so1n", "cflo", "gamma"):
-        assert not np.array(getattr(used, name).ndarray).any(), name
+        assert not np.array(getattr(used, name)[...]).any(), name
     start(used)
     used.march(2)
     fresh = _core(mesh, 2e-3, precision)
