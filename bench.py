@@ -450,7 +450,7 @@ def run_line(args, world, rank, dist):
         from solvcon_gb300 import onedim
         n |= 1
         x, so0, dt = tube_state(n, 2026 + rank)
-        core = onedim.Euler1DCore(n, dt)
+        core = onedim.Euler1DCore(n, dt, precision=args.precision or "fp64")
         core.coord[...] = x
         core.so0[...] = so0
         core.so1.fill(0.0)
@@ -529,8 +529,10 @@ def run_line(args, world, rank, dist):
     e2e_value = world * points * e2e_steps / reduce_max(dist, e2e_s)
 
     hbm_peak, peak_kind = peaks()
-    achieved = LINE_ALG_BYTES[args.workload] * points * args.steps / \
-        (ms.value * 1e-3) / 1e9
+    alg = LINE_ALG_BYTES[args.workload]
+    if args.workload == "tube1d" and args.precision == "fp32":
+        alg = 64  # so0, so1, gamma, cfl in FP32 (56 B), coord FP64 (8 B)
+    achieved = alg * points * args.steps / (ms.value * 1e-3) / 1e9
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         size = args.cpu_nside or cpu_nside(args.workload, args.cpu_steps)
@@ -544,7 +546,8 @@ def run_line(args, world, rank, dist):
         "metric": unit, "value": value, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "f64",
         "data": "synthetic",
         "config": {"workload": "%s (%s)" % (args.workload, desc % n),
                    "points": points, "dt": dt,
@@ -555,8 +558,7 @@ def run_line(args, world, rank, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak,
                      "traffic": None,
-                     "alg_bytes_per_point_step":
-                         LINE_ALG_BYTES[args.workload],
+                     "alg_bytes_per_point_step": alg,
                      "kernel": "one march step (two fused half-step kernels)",
                      "step_ms": ms.value / args.steps,
                      "peak_source": peak_kind},

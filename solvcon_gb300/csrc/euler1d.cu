@@ -29,15 +29,31 @@ namespace
 {
 
 constexpr int B1D = 256;
-constexpr double TINY1D = 1.e-100; // Euler1DKernel::tiny (Euler1DCore.hpp:182)
 
+// Euler1DKernel::tiny (Euler1DCore.hpp:182) in FP64; it underflows in FP32,
+// where the same expressions use the smallest floor that keeps them finite.
+template <typename R>
+struct Tiny1D;
+template <>
+struct Tiny1D<double>
+{
+    static constexpr double V = 1.e-100;
+};
+template <>
+struct Tiny1D<float>
+{
+    static constexpr float V = 1.e-30f;
+};
+
+// Coordinates stay FP64 (the grid); the state, gamma and cfl are R.
+template <typename R>
 struct E1DArgs
 {
     double const * coord;
-    double const * gamma;
-    double * so0; // [n][3]
-    double * so1; // [n][3]
-    double * cfl;
+    R const * gamma;
+    R * so0; // [n][3]
+    R * so1; // [n][3]
+    R * cfl;
     int64_t n;
     double hdt, qdt;
 };
@@ -47,46 +63,55 @@ struct E1DArgs
 // the value up at the point, plus the two half fluxes of calc_flux_ll/lr
 // (Euler1DCore.hpp:246-266).  Reciprocals of rho are formed once: for any
 // density above ~1e-50 the reference's denominators rho^k + tiny equal rho^k.
+// Distances are formed from the FP64 coordinates and then rounded to R.
+template <typename R>
 struct K1D
 {
     double x, xneg, xpos;
-    double r; // 1 / (rho + tiny), shared with update_cfl at the same point
-    double up[3];
-    double ll[3]; // flux through the lower-left of the CE to the right
-    double lr[3]; // flux through the lower-right of the CE to the left
+    R r; // 1 / (rho + tiny), shared with update_cfl at the same point
+    R up[3];
+    R ll[3]; // flux through the lower-left of the CE to the right
+    R lr[3]; // flux through the lower-right of the CE to the left
+    // FP32 delta form: the state u, up - u, and ll / lr without their
+    // dx * u parts (the caller adds those relative to the output point).
+    R u[3];
+    R upd[3];
+    R llp[3];
+    R lrp[3];
 };
 
-__device__ __forceinline__ void derive(E1DArgs const & a, int64_t ic, K1D & k)
+template <typename R>
+__device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> & k)
 {
-    double const ga = a.gamma[ic];
+    R const ga = a.gamma[ic];
     k.x = a.coord[ic];
     k.xneg = a.coord[ic - 1];
     k.xpos = a.coord[ic + 1];
     double const xctr = (k.xpos + k.xneg) * 0.5;
-    double u[3], ux[3];
+    R u[3], ux[3];
     for (int i = 0; i < 3; ++i)
     {
         u[i] = a.so0[ic * 3 + i];
         ux[i] = a.so1[ic * 3 + i];
     }
-    double const r = 1.0 / (u[0] + TINY1D);
+    R const r = R(1) / (u[0] + Tiny1D<R>::V);
     k.r = r;
-    double const r2 = r * r;
-    double const m2r2 = u[1] * u[1] * r2; // u1^2 / u0^2
-    double jac[3][3];
-    jac[0][0] = 0.0;
-    jac[0][1] = 1.0;
-    jac[0][2] = 0.0;
-    jac[1][0] = (ga - 3.0) / 2.0 * m2r2;
-    jac[1][1] = -(ga - 3.0) * u[1] * r;
-    jac[1][2] = ga - 1.0;
-    jac[2][0] = (ga - 1.0) * m2r2 * u[1] * r - ga * u[1] * u[2] * r2;
-    jac[2][1] = ga * u[2] * r - 1.5 * (ga - 1.0) * m2r2;
+    R const r2 = r * r;
+    R const m2r2 = u[1] * u[1] * r2; // u1^2 / u0^2
+    R jac[3][3];
+    jac[0][0] = R(0);
+    jac[0][1] = R(1);
+    jac[0][2] = R(0);
+    jac[1][0] = (ga - R(3)) / R(2) * m2r2;
+    jac[1][1] = -(ga - R(3)) * u[1] * r;
+    jac[1][2] = ga - R(1);
+    jac[2][0] = (ga - R(1)) * m2r2 * u[1] * r - ga * u[1] * u[2] * r2;
+    jac[2][1] = ga * u[2] * r - R(1.5) * (ga - R(1)) * m2r2;
     jac[2][2] = ga * u[1] * r;
-    double f[3], ut[3], ft[3];
+    R f[3], ut[3], ft[3];
     f[0] = u[1];
-    f[1] = (ga - 1.0) * u[2] + (3.0 - ga) / 2.0 * u[1] * u[1] * r;
-    f[2] = ga * u[1] * u[2] * r - (ga - 1.0) / 2.0 * u[1] * m2r2;
+    f[1] = (ga - R(1)) * u[2] + (R(3) - ga) / R(2) * u[1] * u[1] * r;
+    f[2] = ga * u[1] * u[2] * r - (ga - R(1)) / R(2) * u[1] * m2r2;
     for (int i = 0; i < 3; ++i)
     {
         ut[i] = -jac[i][0] * ux[0] - jac[i][1] * ux[1] - jac[i][2] * ux[2];
@@ -95,20 +120,36 @@ __device__ __forceinline__ void derive(E1DArgs const & a, int64_t ic, K1D & k)
     {
         ft[i] = jac[i][0] * ut[0] + jac[i][1] * ut[1] + jac[i][2] * ut[2];
     }
-    double const dxctr = k.x - xctr;
-    for (int i = 0; i < 3; ++i)
+    R const hdt = R(a.hdt), qdt = R(a.qdt);
+    R const dxctr = R(k.x - xctr);
+    R const dxl = R(k.xpos - k.x);
+    R const dml = R(0.5 * (k.x + k.xpos) - xctr);
+    R const dxr = R(k.x - k.xneg);
+    R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
+    if constexpr (sizeof(R) == 4)
     {
-        k.up[i] = u[i] + dxctr * ux[i] + a.hdt * ut[i];
+        for (int i = 0; i < 3; ++i)
+        {
+            k.u[i] = u[i];
+            k.upd[i] = dxctr * ux[i] + hdt * ut[i];
+            k.up[i] = u[i] + k.upd[i]; // for the so1-only half step
+            R const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
+            k.llp[i] = dxl * dml * ux[i] + hdt * tf;
+            k.lrp[i] = dxr * dmr * ux[i] - hdt * tf;
+        }
     }
-    double const dxl = k.xpos - k.x;
-    double const dml = 0.5 * (k.x + k.xpos) - xctr;
-    double const dxr = k.x - k.xneg;
-    double const dmr = 0.5 * (k.x + k.xneg) - xctr;
-    for (int i = 0; i < 3; ++i)
+    else
     {
-        double const tf = f[i] - dxctr * ut[i] + a.qdt * ft[i];
-        k.ll[i] = dxl * (u[i] + dml * ux[i]) + a.hdt * tf;
-        k.lr[i] = dxr * (u[i] + dmr * ux[i]) - a.hdt * tf;
+        for (int i = 0; i < 3; ++i)
+        {
+            k.up[i] = u[i] + dxctr * ux[i] + hdt * ut[i];
+        }
+        for (int i = 0; i < 3; ++i)
+        {
+            R const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
+            k.ll[i] = dxl * (u[i] + dml * ux[i]) + hdt * tf;
+            k.lr[i] = dxr * (u[i] + dmr * ux[i]) - hdt * tf;
+        }
     }
 }
 
@@ -116,116 +157,122 @@ __device__ __forceinline__ void derive(E1DArgs const & a, int64_t ic, K1D & k)
 // divisions by rho use r = 1 / (rho + tiny), the reciprocal the kernel
 // derivation at the same point forms (equal unless rho < ~1e-84, where the
 // reference itself overflows).
-__device__ __forceinline__ double rho_recip(E1DArgs const & a, int64_t it)
+template <typename R>
+__device__ __forceinline__ R rho_recip(E1DArgs<R> const & a, int64_t it)
 {
-    return 1.0 / (a.so0[it * 3 + 0] + TINY1D);
+    return R(1) / (a.so0[it * 3 + 0] + Tiny1D<R>::V);
 }
 
-__device__ __forceinline__ void cfl_at(E1DArgs const & a, int64_t it, double hdt, double r)
+__device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrt_r(float x) { return sqrtf(x); }
+
+template <typename R>
+__device__ __forceinline__ void cfl_at(E1DArgs<R> const & a, int64_t it, double hdt, R r)
 {
-    double const ga = a.gamma[it];
-    double const m = a.so0[it * 3 + 1];
-    double const m2 = m * m;
-    double const ke = 0.5 * m2 * r;
-    double pr = (ga - 1.0) * (a.so0[it * 3 + 2] - ke);
-    pr = (pr + fabs(pr)) / 2.0;
+    R const ga = a.gamma[it];
+    R const m = a.so0[it * 3 + 1];
+    R const m2 = m * m;
+    R const ke = R(0.5) * m2 * r;
+    R pr = (ga - R(1)) * (a.so0[it * 3 + 2] - ke);
+    pr = (pr + fabs(pr)) / R(2);
     // The reference's sqrt(m * m) is |m| exactly: in binary IEEE arithmetic
     // the square root of a correctly rounded square returns the operand's
     // magnitude (barring overflow or underflow of the square).
-    double const wspd = sqrt(ga * pr * r) + fabs(m) * r;
+    R const wspd = sqrt_r(ga * pr * r) + fabs(m) * r;
     double const dxpos = a.coord[it + 1] - a.coord[it];
     double const dxneg = a.coord[it] - a.coord[it - 1];
-    a.cfl[it] = hdt * wspd / (dxpos < dxneg ? dxpos : dxneg);
+    a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
 }
 
 // The W-alpha gradient (march_half_so1_alpha, Euler1DCore.hpp:284-320).
-template <int ALPHA>
-__device__ __forceinline__ double wgrad(double duxn, double duxp)
+template <int ALPHA, typename R>
+__device__ __forceinline__ R wgrad(R duxn, R duxp)
 {
-    double fan = fabs(duxn);
-    double fap = fabs(duxp);
+    R fan = fabs(duxn);
+    R fap = fabs(duxp);
     if constexpr (ALPHA == 2)
     {
         fan *= fan;
         fap *= fap;
     }
-    return (fap * duxn + fan * duxp) / (fap + fan + TINY1D);
+    return (fap * duxn + fan * duxp) / (fap + fan + Tiny1D<R>::V);
 }
 
-// Fused half step: so0, cfl and (when ALPHA > 0) so1 at one parity; with
-// BND also the copy-out boundary treatment (Euler1DCore.cpp:132-172).
-// Output j is point start + 2j + 1 for j < nout; kernels are at start + 2j for
-// j <= nout.
-template <int ALPHA, bool DO_SO0, bool DO_CFL, bool BND>
-__global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t nout)
+// The FP32 half step in delta form: each new so0 is the old value at the
+// point plus the change, formed from the kernels' states relative to it
+// (dxl (u_l - u0) + dxr (u_r - u0) + the flux terms, over dxl + dxr), and the
+// gradient's differences likewise, so FP32 rounding scales with the changes
+// and not with the state.  The copy-out boundary treatment as in k_half.
+template <int ALPHA, bool DO_CFL, bool BND>
+__device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t start, int64_t nout)
 {
-    __shared__ double s_lr[B1D + 1][3];
-    __shared__ double s_up[B1D + 1][3];
-    __shared__ double s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
+    using R = float;
+    __shared__ R s_u[B1D + 1][3];
+    __shared__ R s_upd[B1D + 1][3];
+    __shared__ R s_lrp[B1D + 1][3];
+    __shared__ R s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
     int64_t const j0 = static_cast<int64_t>(blockIdx.x) * B1D;
     int64_t const j = j0 + threadIdx.x;
-    K1D k;
+    K1D<R> k;
     bool const have = j <= nout;
     if (have)
     {
         derive(a, start + 2 * j, k);
         for (int i = 0; i < 3; ++i)
         {
-            s_lr[threadIdx.x][i] = k.lr[i];
-            s_up[threadIdx.x][i] = k.up[i];
+            s_u[threadIdx.x][i] = k.u[i];
+            s_upd[threadIdx.x][i] = k.upd[i];
+            s_lrp[threadIdx.x][i] = k.lrp[i];
         }
-        s_idxr[threadIdx.x] = 1.0 / (k.x - k.xneg);
+        s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
     }
     if (threadIdx.x == 0)
     {
         int64_t const jh = j0 + B1D; // halo kernel on the right
         if (jh <= nout)
         {
-            K1D h;
+            K1D<R> h;
             derive(a, start + 2 * jh, h);
             for (int i = 0; i < 3; ++i)
             {
-                s_lr[B1D][i] = h.lr[i];
-                s_up[B1D][i] = h.up[i];
+                s_u[B1D][i] = h.u[i];
+                s_upd[B1D][i] = h.upd[i];
+                s_lrp[B1D][i] = h.lrp[i];
             }
-            s_idxr[B1D] = 1.0 / (h.x - h.xneg);
+            s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
         }
     }
     __syncthreads();
     if (have && j < nout)
     {
         int64_t const ic = start + 2 * j;
-        double v[3];
-        if (DO_SO0)
+        R const idx = R(1.0 / (a.coord[ic + 2] - a.coord[ic]));
+        R const dxl = R(a.coord[ic + 1] - a.coord[ic]);
+        R const dxr = R(a.coord[ic + 2] - a.coord[ic + 1]);
+        R d[3];
+        for (int i = 0; i < 3; ++i)
         {
-            double const idx = 1.0 / (a.coord[ic + 2] - a.coord[ic]);
-            for (int i = 0; i < 3; ++i)
+            R const u0 = a.so0[(ic + 1) * 3 + i];
+            d[i] = (dxl * (k.u[i] - u0) + dxr * (s_u[threadIdx.x + 1][i] - u0) + k.llp[i] +
+                    s_lrp[threadIdx.x + 1][i]) *
+                   idx;
+            R const v = u0 + d[i];
+            if constexpr (ALPHA > 0)
             {
-                v[i] = (k.ll[i] + s_lr[threadIdx.x + 1][i]) * idx;
-                a.so0[(ic + 1) * 3 + i] = v[i];
+                // The gradient's differences v - up_l and up_r - v, each
+                // from small terms: (u0 - u_l) + d - (up_l - u_l), and
+                // (u_r - u0) + (up_r - u_r) - d.
+                R const idn = R(1.0 / (k.xpos - k.x));
+                R const idp = s_idxr[threadIdx.x + 1];
+                R const duxn = ((u0 - k.u[i]) + d[i] - k.upd[i]) * idn;
+                R const duxp = ((s_u[threadIdx.x + 1][i] - u0) + s_upd[threadIdx.x + 1][i] - d[i]) * idp;
+                a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
             }
-        }
-        else
-        {
-            for (int i = 0; i < 3; ++i)
-            {
-                v[i] = a.so0[(ic + 1) * 3 + i];
-            }
+            a.so0[(ic + 1) * 3 + i] = v;
         }
         if (DO_CFL)
         {
             cfl_at(a, ic, a.hdt, k.r);
-        }
-        if constexpr (ALPHA > 0)
-        {
-            double const idn = 1.0 / (k.xpos - k.x);
-            double const idp = s_idxr[threadIdx.x + 1];
-            for (int i = 0; i < 3; ++i)
-            {
-                double const duxn = (v[i] - k.up[i]) * idn;
-                double const duxp = (s_up[threadIdx.x + 1][i] - v[i]) * idp;
-                a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
-            }
         }
     }
     if (BND && blockIdx.x == 0 && threadIdx.x == 0)
@@ -241,8 +288,106 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs a, int64_t start, int64_t 
     }
 }
 
+// Fused half step: so0, cfl and (when ALPHA > 0) so1 at one parity; with
+// BND also the copy-out boundary treatment (Euler1DCore.cpp:132-172).
+// Output j is point start + 2j + 1 for j < nout; kernels are at start + 2j for
+// j <= nout.
+template <int ALPHA, bool DO_SO0, bool DO_CFL, bool BND, typename R>
+__global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64_t nout)
+{
+    if constexpr (sizeof(R) == 4 && DO_SO0)
+    {
+        half_delta<ALPHA, DO_CFL, BND>(a, start, nout);
+    }
+    else
+    {
+        __shared__ R s_lr[B1D + 1][3];
+        __shared__ R s_up[B1D + 1][3];
+        __shared__ R s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
+        int64_t const j0 = static_cast<int64_t>(blockIdx.x) * B1D;
+        int64_t const j = j0 + threadIdx.x;
+        K1D<R> k;
+        bool const have = j <= nout;
+        if (have)
+        {
+            derive(a, start + 2 * j, k);
+            for (int i = 0; i < 3; ++i)
+            {
+                s_lr[threadIdx.x][i] = k.lr[i];
+                s_up[threadIdx.x][i] = k.up[i];
+            }
+            s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
+        }
+        if (threadIdx.x == 0)
+        {
+            int64_t const jh = j0 + B1D; // halo kernel on the right
+            if (jh <= nout)
+            {
+                K1D<R> h;
+                derive(a, start + 2 * jh, h);
+                for (int i = 0; i < 3; ++i)
+                {
+                    s_lr[B1D][i] = h.lr[i];
+                    s_up[B1D][i] = h.up[i];
+                }
+                s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
+            }
+        }
+        __syncthreads();
+        if (have && j < nout)
+        {
+            int64_t const ic = start + 2 * j;
+            R v[3];
+            if (DO_SO0)
+            {
+                R const idx = R(1.0 / (a.coord[ic + 2] - a.coord[ic]));
+                for (int i = 0; i < 3; ++i)
+                {
+                    v[i] = (k.ll[i] + s_lr[threadIdx.x + 1][i]) * idx;
+                    a.so0[(ic + 1) * 3 + i] = v[i];
+                }
+            }
+            else
+            {
+                for (int i = 0; i < 3; ++i)
+                {
+                    v[i] = a.so0[(ic + 1) * 3 + i];
+                }
+            }
+            if (DO_CFL)
+            {
+                cfl_at(a, ic, a.hdt, k.r);
+            }
+            if constexpr (ALPHA > 0)
+            {
+                R const idn = R(1.0 / (k.xpos - k.x));
+                R const idp = s_idxr[threadIdx.x + 1];
+                for (int i = 0; i < 3; ++i)
+                {
+                    R const duxn = (v[i] - k.up[i]) * idn;
+                    R const duxp = (s_up[threadIdx.x + 1][i] - v[i]) * idp;
+                    a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
+                }
+            }
+        }
+        if (BND && blockIdx.x == 0 && threadIdx.x == 0)
+        {
+            int64_t const l = 1, r = a.n - 2;
+            for (int i = 0; i < 3; ++i)
+            {
+                a.so0[l * 3 + i] = a.so0[(l + 1) * 3 + i];
+                a.so0[r * 3 + i] = a.so0[(r - 1) * 3 + i];
+                a.so1[l * 3 + i] = a.so1[(l + 1) * 3 + i];
+                a.so1[r * 3 + i] = a.so1[(r - 1) * 3 + i];
+            }
+        }
+
+    }
+}
+
 // update_cfl alone.
-__global__ void k_cfl1d(E1DArgs a, int64_t start, int64_t nout)
+template <typename R>
+__global__ void k_cfl1d(E1DArgs<R> a, int64_t start, int64_t nout)
 {
     int64_t const j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j < nout)
@@ -253,10 +398,11 @@ __global__ void k_cfl1d(E1DArgs a, int64_t start, int64_t nout)
 }
 
 // treat_boundary_so0 / treat_boundary_so1.
-__global__ void k_bnd1d(E1DArgs a, int which)
+template <typename R>
+__global__ void k_bnd1d(E1DArgs<R> a, int which)
 {
     int64_t const l = 1, r = a.n - 2;
-    double * s = which == 0 ? a.so0 : a.so1;
+    R * s = which == 0 ? a.so0 : a.so1;
     for (int i = 0; i < 3; ++i)
     {
         s[l * 3 + i] = s[(l + 1) * 3 + i];
@@ -264,13 +410,56 @@ __global__ void k_bnd1d(E1DArgs a, int which)
     }
 }
 
-class Euler1D
+// FP64 host tables to and from the FP32 state, converted on the device; the
+// host side read or written in place when it is a mapped scg_host_alloc
+// block, else through a device staging table.
+__global__ void k_e1d_from_f64(double const * in, float * out, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        out[i] = float(in[i]);
+    }
+}
+
+__global__ void k_e1d_to_f64(float const * in, double * out, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        out[i] = double(in[i]);
+    }
+}
+
+// What the C ABI calls on a 1D core of either precision.
+struct Euler1DBase
+{
+    virtual ~Euler1DBase() = default;
+    virtual std::unique_ptr<Euler1DBase> clone() = 0;
+    virtual int64_t count(int which) const = 0;
+    virtual void get(int which, double * host) = 0;
+    virtual void set(int which, double const * host) = 0;
+    virtual void op(int which, int odd, int alpha) = 0;
+    virtual void march(int alpha, int64_t steps) = 0;
+    virtual void sync() = 0;
+    int64_t n = 0;
+    double time_increment = 0.0;
+    int precision = SCG_FP64;
+    cudaStream_t stream = nullptr;
+};
+
+// R = double: the reference's arithmetic; R = float: FP32 state, cfl and
+// gamma, with the grid (coordinates and the distances formed from them) in
+// FP64 and rounded once.
+template <typename R>
+class Euler1D : public Euler1DBase
 {
 public:
     Euler1D(int64_t ncoord, double dt)
-        : n(ncoord)
-        , time_increment(dt)
     {
+        n = ncoord;
+        time_increment = dt;
+        precision = sizeof(R) == 8 ? SCG_FP64 : SCG_FP32;
         if (ncoord % 2 == 0)
         {
             throw std::invalid_argument("ncoord cannot be even");
@@ -280,21 +469,21 @@ public:
             throw std::invalid_argument("Euler1DCore: ncoord must be at least 5");
         }
         scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        for (auto * b : {&coord, &cfl, &gamma})
+        coord.alloc(static_cast<size_t>(n));
+        for (auto * b : {&cfl, &gamma})
             b->alloc(static_cast<size_t>(n));
         so0.alloc(static_cast<size_t>(n * 3));
         so1.alloc(static_cast<size_t>(n * 3));
         std::vector<double> g(static_cast<size_t>(n), 1.4);
         std::vector<double> z(static_cast<size_t>(n * 3), 0.0);
-        put(gamma.ptr, g.data(), n);
-        put(coord.ptr, z.data(), n);
-        put(cfl.ptr, z.data(), n);
-        put(so0.ptr, z.data(), n * 3);
-        put(so1.ptr, z.data(), n * 3);
-        sync();
+        set(4, g.data());
+        set(0, z.data());
+        set(1, z.data());
+        set(2, z.data());
+        set(3, z.data());
     }
 
-    ~Euler1D()
+    ~Euler1D() override
     {
         if (graph_exec)
             cudaGraphExecDestroy(graph_exec);
@@ -305,26 +494,27 @@ public:
         }
     }
 
-    std::unique_ptr<Euler1D> clone()
+    std::unique_ptr<Euler1DBase> clone() override
     {
-        auto c = std::make_unique<Euler1D>(n, time_increment);
-        for (int k = 0; k < 5; ++k)
+        auto c = std::make_unique<Euler1D<R>>(n, time_increment);
+        scg::cuda_check(cudaMemcpyAsync(c->coord.ptr, coord.ptr, sizeof(double) * static_cast<size_t>(n),
+                                        cudaMemcpyDeviceToDevice, stream),
+                        "copy");
+        for (int k = 1; k < 5; ++k)
         {
-            double * src = field(k);
-            double * dst = c->field(k);
-            size_t const cnt = static_cast<size_t>(k >= 2 && k <= 3 ? n * 3 : n);
-            scg::cuda_check(cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+            size_t const cnt = static_cast<size_t>(count(k));
+            scg::cuda_check(cudaMemcpyAsync(c->state(k), state(k), cnt * sizeof(R), cudaMemcpyDeviceToDevice, stream),
+                            "copy");
         }
         sync();
         return c;
     }
 
-    // 0 coord, 1 cfl, 2 so0, 3 so1, 4 gamma
-    double * field(int which)
+    // 0 coord (FP64), 1 cfl, 2 so0, 3 so1, 4 gamma (R)
+    R * state(int which)
     {
         switch (which)
         {
-        case 0: return coord.ptr;
         case 1: return cfl.ptr;
         case 2: return so0.ptr;
         case 3: return so1.ptr;
@@ -332,25 +522,92 @@ public:
         default: throw std::invalid_argument("Euler1DCore: unknown array id " + std::to_string(which));
         }
     }
-    int64_t count(int which) const { return (which == 2 || which == 3) ? n * 3 : n; }
+    int64_t count(int which) const override { return (which == 2 || which == 3) ? n * 3 : n; }
 
-    void get(int which, double * host)
+    void get(int which, double * host) override
     {
-        scg::cuda_check(cudaMemcpyAsync(host, field(which), sizeof(double) * static_cast<size_t>(count(which)),
-                                        cudaMemcpyDeviceToHost, stream),
-                        "D2H");
-        sync();
+        size_t const cnt = static_cast<size_t>(count(which));
+        if (which == 0)
+        {
+            scg::cuda_check(cudaMemcpyAsync(host, coord.ptr, sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
+                            "D2H");
+            sync();
+            return;
+        }
+        if constexpr (sizeof(R) == 8)
+        {
+            scg::cuda_check(cudaMemcpyAsync(host, state(which), sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
+                            "D2H");
+            sync();
+        }
+        else
+        {
+            unsigned const grid = static_cast<unsigned>((cnt + 255) / 256);
+            if (double * const dev = static_cast<double *>(scg::mapped_host(host, sizeof(double) * cnt)))
+            {
+                k_e1d_to_f64<<<grid, 256, 0, stream>>>(state(which), dev, static_cast<int64_t>(cnt));
+                scg::launched(stream, "e1d_to_f64");
+            }
+            else
+            {
+                double * const tmp = staging(cnt);
+                k_e1d_to_f64<<<grid, 256, 0, stream>>>(state(which), tmp, static_cast<int64_t>(cnt));
+                scg::launched(stream, "e1d_to_f64");
+                scg::cuda_check(cudaMemcpyAsync(host, tmp, sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
+                                "D2H");
+            }
+            sync();
+        }
     }
-    void set(int which, double const * host)
+    void set(int which, double const * host) override
     {
-        put(field(which), host, count(which));
-        sync();
+        size_t const cnt = static_cast<size_t>(count(which));
+        if (which == 0)
+        {
+            put(coord.ptr, host, cnt);
+            return;
+        }
+        if constexpr (sizeof(R) == 8)
+        {
+            put(state(which), host, cnt);
+        }
+        else
+        {
+            unsigned const grid = static_cast<unsigned>((cnt + 255) / 256);
+            if (double const * const dev =
+                    static_cast<double const *>(scg::mapped_host(host, sizeof(double) * cnt)))
+            {
+                k_e1d_from_f64<<<grid, 256, 0, stream>>>(dev, state(which), static_cast<int64_t>(cnt));
+                scg::launched(stream, "e1d_from_f64");
+            }
+            else
+            {
+                double * const tmp = staging(cnt);
+                scg::cuda_check(cudaMemcpyAsync(tmp, host, sizeof(double) * cnt, cudaMemcpyHostToDevice, stream),
+                                "H2D");
+                k_e1d_from_f64<<<grid, 256, 0, stream>>>(tmp, state(which), static_cast<int64_t>(cnt));
+                scg::launched(stream, "e1d_from_f64");
+            }
+            sync();
+        }
     }
 
-    E1DArgs args()
+    // Grow-only device table for FP64 host data on its way to or from the
+    // FP32 state.
+    double * staging(size_t cnt)
     {
-        return E1DArgs{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
-                       time_increment / 4.0};
+        if (m_staging.n < cnt)
+        {
+            sync();
+            m_staging.alloc(cnt);
+        }
+        return m_staging.ptr;
+    }
+
+    E1DArgs<R> args()
+    {
+        return E1DArgs<R>{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
+                          time_increment / 4.0};
     }
 
     // Loop bounds of a half step (Euler1DCore.cpp:73-74, 99-100).
@@ -367,11 +624,11 @@ public:
         int64_t start, nout;
         range(odd, start, nout);
         unsigned const grid = static_cast<unsigned>((nout + B1D) / B1D);
-        k_half<ALPHA, SO0, CFL, BND><<<grid, B1D, 0, stream>>>(args(), start, nout);
+        k_half<ALPHA, SO0, CFL, BND, R><<<grid, B1D, 0, stream>>>(args(), start, nout);
         scg::launched(stream, "e1d_half");
     }
 
-    void op(int which, int odd, int alpha)
+    void op(int which, int odd, int alpha) override
     {
         switch (which)
         {
@@ -381,7 +638,7 @@ public:
             range(odd != 0, start, nout);
             if (nout > 0)
             {
-                k_cfl1d<<<static_cast<unsigned>((nout + 255) / 256), 256, 0, stream>>>(args(), start, nout);
+                k_cfl1d<R><<<static_cast<unsigned>((nout + 255) / 256), 256, 0, stream>>>(args(), start, nout);
                 scg::launched(stream, "e1d_cfl");
             }
             break;
@@ -397,7 +654,7 @@ public:
             break;
         case 3: // treat_boundary_so0
         case 4: // treat_boundary_so1
-            k_bnd1d<<<1, 1, 0, stream>>>(args(), which - 3);
+            k_bnd1d<R><<<1, 1, 0, stream>>>(args(), which - 3);
             scg::launched(stream, "e1d_bnd");
             break;
         case 5: // setup_march
@@ -406,7 +663,7 @@ public:
             range(false, start, nout);
             if (nout > 0)
             {
-                k_cfl1d<<<static_cast<unsigned>((nout + 255) / 256), 256, 0, stream>>>(args(), start, nout);
+                k_cfl1d<R><<<static_cast<unsigned>((nout + 255) / 256), 256, 0, stream>>>(args(), start, nout);
                 scg::launched(stream, "e1d_cfl");
             }
             break;
@@ -447,7 +704,7 @@ public:
 
     // march_alpha(steps): chunks of GRAPH_STEPS steps replay one captured
     // CUDA graph; the remainder launches directly.
-    void march(int alpha, int64_t steps)
+    void march(int alpha, int64_t steps) override
     {
         if (alpha != 1 && alpha != 2)
         {
@@ -494,24 +751,21 @@ public:
         graph_alpha = alpha;
     }
 
-    void sync() { scg::cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
-
-    int64_t n;
-    double time_increment;
-    cudaStream_t stream = nullptr;
+    void sync() override { scg::cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
 
 private:
     static constexpr int GRAPH_STEPS = 32;
 
-    void put(double * dst, double const * src, int64_t cnt)
+    template <typename T>
+    void put(T * dst, T const * src, size_t cnt)
     {
-        scg::cuda_check(cudaMemcpyAsync(dst, src, sizeof(double) * static_cast<size_t>(cnt), cudaMemcpyHostToDevice,
-                                        stream),
-                        "H2D");
+        scg::cuda_check(cudaMemcpyAsync(dst, src, sizeof(T) * cnt, cudaMemcpyHostToDevice, stream), "H2D");
         sync();
     }
 
-    scg::DevBuf<double> coord, cfl, so0, so1, gamma;
+    scg::DevBuf<double> coord;
+    scg::DevBuf<R> cfl, so0, so1, gamma;
+    scg::DevBuf<double> m_staging;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
 };
@@ -520,7 +774,7 @@ private:
 
 struct scg_e1d
 {
-    std::unique_ptr<Euler1D> c;
+    std::unique_ptr<Euler1DBase> c;
 };
 
 extern "C"
@@ -528,11 +782,26 @@ extern "C"
 
 int scg_e1d_create(int64_t ncoord, double time_increment, scg_e1d ** out)
 {
+    return scg_e1d_create_precision(ncoord, time_increment, SCG_FP64, out);
+}
+
+int scg_e1d_create_precision(int64_t ncoord, double time_increment, int precision, scg_e1d ** out)
+{
     return scg::guarded([&] {
         auto h = std::make_unique<scg_e1d>();
-        h->c = std::make_unique<Euler1D>(ncoord, time_increment);
+        if (precision == SCG_FP64)
+            h->c = std::make_unique<Euler1D<double>>(ncoord, time_increment);
+        else if (precision == SCG_FP32)
+            h->c = std::make_unique<Euler1D<float>>(ncoord, time_increment);
+        else
+            throw std::invalid_argument("Euler1DCore: precision must be SCG_FP64 or SCG_FP32");
         *out = h.release();
     });
+}
+
+int scg_e1d_precision(const scg_e1d * h, int * precision)
+{
+    return scg::guarded([&] { *precision = h->c->precision; });
 }
 
 int scg_e1d_destroy(scg_e1d * h)

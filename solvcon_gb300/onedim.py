@@ -23,6 +23,9 @@ __all__ = ["Euler1DCore", "Euler1DSolver", "ShockTube"]
 _vp = ctypes.c_void_p
 lib = _lib.bind_more({
     "scg_e1d_create": ([ctypes.c_int64, ctypes.c_double, _vp], ctypes.c_int),
+    "scg_e1d_create_precision": ([ctypes.c_int64, ctypes.c_double,
+                                  ctypes.c_int, _vp], ctypes.c_int),
+    "scg_e1d_precision": ([_vp, _vp], ctypes.c_int),
     "scg_e1d_destroy": ([_vp], ctypes.c_int),
     "scg_e1d_clone": ([_vp, _vp], ctypes.c_int),
     "scg_e1d_info": ([_vp, _vp, _vp], ctypes.c_int),
@@ -40,16 +43,29 @@ R_GAS = 8.31446261815324  # Euler1DCore::R (Euler1DCore.hpp:48)
 TINY = 1.e-100            # Euler1DCore::TINY (Euler1DCore.hpp:47)
 
 
+_E1D_PRECISIONS = {"fp64": 0, "fp32": 2}
+
+
 class Euler1DCore:
-    """1D Euler CESE core on the GPU (Euler1DCore.hpp:39-142)."""
+    """1D Euler CESE core on the GPU (Euler1DCore.hpp:39-142).
+
+    :param precision: ``"fp64"`` (the reference's arithmetic) or ``"fp32"``
+        (FP32 state, CFL and gamma with the grid kept FP64; not in the
+        reference).
+    """
 
     nvar = 3
 
-    def __init__(self, ncoord, time_increment, _handle=None):
+    def __init__(self, ncoord, time_increment, precision="fp64",
+                 _handle=None):
         h = ctypes.c_void_p()
         if _handle is None:
-            check(lib.scg_e1d_create(int(ncoord), float(time_increment),
-                                     ctypes.byref(h)))
+            if precision not in _E1D_PRECISIONS:
+                raise ValueError("Euler1DCore: precision must be one of %s"
+                                 % sorted(_E1D_PRECISIONS))
+            check(lib.scg_e1d_create_precision(
+                int(ncoord), float(time_increment),
+                _E1D_PRECISIONS[precision], ctypes.byref(h)))
         else:
             h = _handle
         self._h = h
@@ -57,6 +73,10 @@ class Euler1DCore:
         dt = ctypes.c_double()
         check(lib.scg_e1d_info(h, ctypes.byref(n), ctypes.byref(dt)))
         self._n, self._dt = n.value, dt.value
+        code = ctypes.c_int()
+        check(lib.scg_e1d_precision(h, ctypes.byref(code)))
+        self._precision = {v: k for k, v in _E1D_PRECISIONS.items()}[
+            code.value]
         self._cache = {}
         self._valid = set()
         self._dirty = set()
@@ -80,6 +100,7 @@ class Euler1DCore:
 
     ncoord = property(lambda self: self._n)
     time_increment = property(lambda self: self._dt)
+    precision = property(lambda self: self._precision)
 
     # -- host mirror (same coherence rules as multidim.EulerCore) -----------
 

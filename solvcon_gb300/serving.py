@@ -115,7 +115,8 @@ class Server:
     :param max_chunk: most steps one tick advances (measured on the mixed
         workload of 1D tubes and 2D meshes: 32 gave 3.68 G cell-steps/s
         aggregate, 16 gave 3.28, 64 3.46, 128 3.30, 256 3.12).
-    :param precision: precision of the 2D solves.
+    :param precision: precision of the 2D solves; the 1D tubes run in FP32
+        state for either FP32 form and in FP64 otherwise.
     """
 
     def __init__(self, hbm_budget=120 * 2 ** 30, max_chunk=32,
@@ -183,7 +184,9 @@ class Server:
             est = self.tube_bytes(req.ncoord)
             if not self._evict_idle(est):
                 return None
-            slot = _Slot(key, Euler1DCore(req.ncoord, tube_dt(req.ncoord)),
+            slot = _Slot(key, Euler1DCore(req.ncoord, tube_dt(req.ncoord),
+                                          precision=_tube_precision(
+                                              self.precision)),
                          est)
         self.held += slot.nbytes
         self.slots[key].append(slot)
@@ -323,6 +326,12 @@ def stats(finished, makespan):
             "cell_steps_per_s": work / makespan}
 
 
+def _tube_precision(precision):
+    """The 1D cores' precision for a server of the given 2D precision: FP32
+    state for either FP32 form, else the reference's FP64."""
+    return "fp64" if precision == "fp64" else "fp32"
+
+
 def alone(server, req, precision):
     """March one request alone (its own solver, its own launches) and return
     (result, seconds)."""
@@ -341,7 +350,7 @@ def alone(server, req, precision):
         secs = time.perf_counter() - t0
         return np.array(core.so0n[...])[core.ngstcell:], secs
     x, so0, dt = sod_tube_state(req.ncoord, req.seed)
-    tube = Euler1DCore(req.ncoord, dt)
+    tube = Euler1DCore(req.ncoord, dt, precision=_tube_precision(precision))
     tube.coord[...] = x
     tube.so0[...] = so0
     tube.so1.fill(0.0)
