@@ -549,7 +549,10 @@ def run_line(args, world, rank, dist):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "fp32" else "f64",
         "data": "synthetic",
-        "config": {"workload": "%s (%s)" % (args.workload, desc % n),
+        "config": {"workload": "%s (%s)" % (
+                       args.workload, (desc % n).replace(
+                           "FP64", "FP32 state, FP64 coordinates")
+                       if args.precision == "fp32" else desc % n),
                    "points": points, "dt": dt,
                    "l2": "state larger than L2 (no flush needed)"
                    if points * LINE_ALG_BYTES[args.workload] > 2e8 else
@@ -801,7 +804,7 @@ def run_serve(args, world, rank, dist):
         "metric": "cell-steps/s", "value": best["cell_steps_per_s"],
         "unit": "cell-steps/s", "n_gpus": world, "steps": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (2D) / f64 (1D)", "data": "synthetic",
+        "dtype": "f32", "data": "synthetic",
         "config": {"workload": "serve (%d requests per rate: 30%% 1D Sod-type "
                                "tubes of 1k-100k points, 70%% 2D meshes of "
                                "the batched distribution, 200-2000 steps; "

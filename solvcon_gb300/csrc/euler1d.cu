@@ -56,6 +56,11 @@ struct E1DArgs
     R * cfl;
     int64_t n;
     double hdt, qdt;
+    // FP32 core: the grid spacing of each point, x - xneg and xpos - x,
+    // formed in FP64 from the coordinates once; and dt/2, dt/4 in R.
+    float const * dxm;
+    float const * dxp;
+    R hdt_r, qdt_r;
 };
 
 // The solution-element kernel at point ic (Euler1DKernel::set_value and
@@ -78,16 +83,25 @@ struct K1D
     R upd[3];
     R llp[3];
     R lrp[3];
+    R dm, dp; // FP32: x - xneg, xpos - x
 };
 
 template <typename R>
 __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> & k)
 {
     R const ga = a.gamma[ic];
-    k.x = a.coord[ic];
-    k.xneg = a.coord[ic - 1];
-    k.xpos = a.coord[ic + 1];
-    double const xctr = (k.xpos + k.xneg) * 0.5;
+    double xctr = 0.0;
+    if constexpr (sizeof(R) == 8)
+    {
+        k.x = a.coord[ic];
+        k.xneg = a.coord[ic - 1];
+        k.xpos = a.coord[ic + 1];
+        xctr = (k.xpos + k.xneg) * 0.5;
+    }
+    else
+    {
+        k.x = k.xneg = k.xpos = 0.0; // the FP32 path works from dm, dp
+    }
     R u[3], ux[3];
     for (int i = 0; i < 3; ++i)
     {
@@ -120,14 +134,21 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
     {
         ft[i] = jac[i][0] * ut[0] + jac[i][1] * ut[1] + jac[i][2] * ut[2];
     }
-    R const hdt = R(a.hdt), qdt = R(a.qdt);
-    R const dxctr = R(k.x - xctr);
-    R const dxl = R(k.xpos - k.x);
-    R const dml = R(0.5 * (k.x + k.xpos) - xctr);
-    R const dxr = R(k.x - k.xneg);
-    R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
     if constexpr (sizeof(R) == 4)
     {
+        // All in FP32 from the point's spacing: with dm = x - xneg and
+        // dp = xpos - x, x - xctr = (dm - dp) / 2, and the BCE midpoints
+        // sit at dm / 2 and -dp / 2 from the centre.
+        R const hdt = a.hdt_r, qdt = a.qdt_r;
+        R const dm = a.dxm[ic];
+        R const dp = a.dxp[ic];
+        k.dm = dm;
+        k.dp = dp;
+        R const dxctr = R(0.5) * (dm - dp);
+        R const dxl = dp;
+        R const dml = R(0.5) * dm;
+        R const dxr = dm;
+        R const dmr = R(-0.5) * dp;
         for (int i = 0; i < 3; ++i)
         {
             k.u[i] = u[i];
@@ -140,6 +161,12 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
     }
     else
     {
+        R const hdt = R(a.hdt), qdt = R(a.qdt);
+        R const dxctr = R(k.x - xctr);
+        R const dxl = R(k.xpos - k.x);
+        R const dml = R(0.5 * (k.x + k.xpos) - xctr);
+        R const dxr = R(k.x - k.xneg);
+        R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
         for (int i = 0; i < 3; ++i)
         {
             k.up[i] = u[i] + dxctr * ux[i] + hdt * ut[i];
@@ -179,9 +206,18 @@ __device__ __forceinline__ void cfl_at(E1DArgs<R> const & a, int64_t it, double 
     // the square root of a correctly rounded square returns the operand's
     // magnitude (barring overflow or underflow of the square).
     R const wspd = sqrt_r(ga * pr * r) + fabs(m) * r;
-    double const dxpos = a.coord[it + 1] - a.coord[it];
-    double const dxneg = a.coord[it] - a.coord[it - 1];
-    a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
+    if constexpr (sizeof(R) == 4)
+    {
+        R const dxpos = a.dxp[it];
+        R const dxneg = a.dxm[it];
+        a.cfl[it] = a.hdt_r * wspd / (dxpos < dxneg ? dxpos : dxneg);
+    }
+    else
+    {
+        double const dxpos = a.coord[it + 1] - a.coord[it];
+        double const dxneg = a.coord[it] - a.coord[it - 1];
+        a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
+    }
 }
 
 // The W-alpha gradient (march_half_so1_alpha, Euler1DCore.hpp:284-320).
@@ -210,7 +246,7 @@ __device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t sta
     __shared__ R s_u[B1D + 1][3];
     __shared__ R s_upd[B1D + 1][3];
     __shared__ R s_lrp[B1D + 1][3];
-    __shared__ R s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
+    __shared__ R s_dm[B1D + 1]; // x - xneg of each kernel
     int64_t const j0 = static_cast<int64_t>(blockIdx.x) * B1D;
     int64_t const j = j0 + threadIdx.x;
     K1D<R> k;
@@ -224,7 +260,7 @@ __device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t sta
             s_upd[threadIdx.x][i] = k.upd[i];
             s_lrp[threadIdx.x][i] = k.lrp[i];
         }
-        s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
+        s_dm[threadIdx.x] = k.dm;
     }
     if (threadIdx.x == 0)
     {
@@ -239,16 +275,17 @@ __device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t sta
                 s_upd[B1D][i] = h.upd[i];
                 s_lrp[B1D][i] = h.lrp[i];
             }
-            s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
+            s_dm[B1D] = h.dm;
         }
     }
     __syncthreads();
     if (have && j < nout)
     {
         int64_t const ic = start + 2 * j;
-        R const idx = R(1.0 / (a.coord[ic + 2] - a.coord[ic]));
-        R const dxl = R(a.coord[ic + 1] - a.coord[ic]);
-        R const dxr = R(a.coord[ic + 2] - a.coord[ic + 1]);
+        // The output point ic + 1 between kernels ic (left) and ic + 2.
+        R const dxl = k.dp;
+        R const dxr = s_dm[threadIdx.x + 1];
+        R const idx = R(1) / (dxl + dxr);
         R d[3];
         for (int i = 0; i < 3; ++i)
         {
@@ -262,8 +299,8 @@ __device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t sta
                 // The gradient's differences v - up_l and up_r - v, each
                 // from small terms: (u0 - u_l) + d - (up_l - u_l), and
                 // (u_r - u0) + (up_r - u_r) - d.
-                R const idn = R(1.0 / (k.xpos - k.x));
-                R const idp = s_idxr[threadIdx.x + 1];
+                R const idn = R(1) / dxl;
+                R const idp = R(1) / dxr;
                 R const duxn = ((u0 - k.u[i]) + d[i] - k.upd[i]) * idn;
                 R const duxp = ((s_u[threadIdx.x + 1][i] - u0) + s_upd[threadIdx.x + 1][i] - d[i]) * idp;
                 a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
@@ -316,7 +353,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                 s_lr[threadIdx.x][i] = k.lr[i];
                 s_up[threadIdx.x][i] = k.up[i];
             }
-            s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
+            s_idxr[threadIdx.x] = sizeof(R) == 4 ? R(1) / k.dm : R(1.0 / (k.x - k.xneg));
         }
         if (threadIdx.x == 0)
         {
@@ -330,7 +367,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                     s_lr[B1D][i] = h.lr[i];
                     s_up[B1D][i] = h.up[i];
                 }
-                s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
+                s_idxr[B1D] = sizeof(R) == 4 ? R(1) / h.dm : R(1.0 / (h.x - h.xneg));
             }
         }
         __syncthreads();
@@ -360,7 +397,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
             }
             if constexpr (ALPHA > 0)
             {
-                R const idn = R(1.0 / (k.xpos - k.x));
+                R const idn = sizeof(R) == 4 ? R(1) / k.dp : R(1.0 / (k.xpos - k.x));
                 R const idp = s_idxr[threadIdx.x + 1];
                 for (int i = 0; i < 3; ++i)
                 {
@@ -431,6 +468,18 @@ __global__ void k_e1d_to_f64(float const * in, double * out, int64_t n)
     }
 }
 
+// The FP32 core's grid spacing, x - xneg and xpos - x, formed in FP64 from the
+// coordinates and rounded once (zero where a neighbour is missing).
+__global__ void k_e1d_spacing(double const * coord, float * dxm, float * dxp, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        dxm[i] = i > 0 ? float(coord[i] - coord[i - 1]) : 0.f;
+        dxp[i] = i + 1 < n ? float(coord[i + 1] - coord[i]) : 0.f;
+    }
+}
+
 // What the C ABI calls on a 1D core of either precision.
 struct Euler1DBase
 {
@@ -449,8 +498,8 @@ struct Euler1DBase
 };
 
 // R = double: the reference's arithmetic; R = float: FP32 state, cfl and
-// gamma, with the grid (coordinates and the distances formed from them) in
-// FP64 and rounded once.
+// gamma, with the coordinates kept in FP64 and the spacing between them
+// formed in FP64 and rounded once to FP32 tables (dxm, dxp).
 template <typename R>
 class Euler1D : public Euler1DBase
 {
@@ -474,6 +523,11 @@ public:
             b->alloc(static_cast<size_t>(n));
         so0.alloc(static_cast<size_t>(n * 3));
         so1.alloc(static_cast<size_t>(n * 3));
+        if constexpr (sizeof(R) == 4)
+        {
+            dxm.alloc(static_cast<size_t>(n));
+            dxp.alloc(static_cast<size_t>(n));
+        }
         std::vector<double> g(static_cast<size_t>(n), 1.4);
         std::vector<double> z(static_cast<size_t>(n * 3), 0.0);
         set(4, g.data());
@@ -507,6 +561,7 @@ public:
                             "copy");
         }
         sync();
+        c->spacing();
         return c;
     }
 
@@ -565,6 +620,7 @@ public:
         if (which == 0)
         {
             put(coord.ptr, host, cnt);
+            spacing();
             return;
         }
         if constexpr (sizeof(R) == 8)
@@ -592,6 +648,18 @@ public:
         }
     }
 
+    // The FP32 core's spacing tables from the coordinates, after each write
+    // of them.
+    void spacing()
+    {
+        if constexpr (sizeof(R) == 4)
+        {
+            k_e1d_spacing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(coord.ptr, dxm.ptr, dxp.ptr, n);
+            scg::launched(stream, "e1d_spacing");
+            sync();
+        }
+    }
+
     // Grow-only device table for FP64 host data on its way to or from the
     // FP32 state.
     double * staging(size_t cnt)
@@ -606,8 +674,18 @@ public:
 
     E1DArgs<R> args()
     {
-        return E1DArgs<R>{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
-                          time_increment / 4.0};
+        return E1DArgs<R>{coord.ptr,
+                          gamma.ptr,
+                          so0.ptr,
+                          so1.ptr,
+                          cfl.ptr,
+                          n,
+                          time_increment / 2.0,
+                          time_increment / 4.0,
+                          dxm.ptr,
+                          dxp.ptr,
+                          R(time_increment / 2.0),
+                          R(time_increment / 4.0)};
     }
 
     // Loop bounds of a half step (Euler1DCore.cpp:73-74, 99-100).
@@ -765,6 +843,7 @@ private:
 
     scg::DevBuf<double> coord;
     scg::DevBuf<R> cfl, so0, so1, gamma;
+    scg::DevBuf<float> dxm, dxp; // the FP32 core's grid spacing
     scg::DevBuf<double> m_staging;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
