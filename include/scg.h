@@ -274,7 +274,8 @@ int scg_euler_profile_stats(scg_euler * core, double * ms_total, int64_t * launc
 /* Euler1DCore(ncoord, time_increment): Euler1DCore.hpp:71-75, Euler1DCore.cpp:22-35. */
 int scg_e1d_create(int64_t ncoord, double time_increment, scg_e1d ** out);
 /* The same with the state precision: SCG_FP64 (the reference's arithmetic)
- * or SCG_FP32 (FP32 state, cfl and gamma; the grid kept FP64).  Not in the
+ * or SCG_FP32 (FP32 state, cfl and gamma; coordinates kept FP64, the spacing
+ * between them formed in FP64 and rounded once to FP32).  Not in the
  * reference. */
 int scg_e1d_create_precision(int64_t ncoord, double time_increment, int precision, scg_e1d ** out);
 int scg_e1d_precision(const scg_e1d * h, int * precision);

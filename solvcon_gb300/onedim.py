@@ -50,8 +50,9 @@ class Euler1DCore:
     """1D Euler CESE core on the GPU (Euler1DCore.hpp:39-142).
 
     :param precision: ``"fp64"`` (the reference's arithmetic) or ``"fp32"``
-        (FP32 state, CFL and gamma with the grid kept FP64; not in the
-        reference).
+        (FP32 state, CFL and gamma, marched in delta form; coordinates
+        kept FP64 and the spacing between them rounded once to FP32; not
+        in the reference).
     """
 
     nvar = 3
