@@ -68,7 +68,8 @@ struct E1DArgs
 // the value up at the point, plus the two half fluxes of calc_flux_ll/lr
 // (Euler1DCore.hpp:246-266).  Reciprocals of rho are formed once: for any
 // density above ~1e-50 the reference's denominators rho^k + tiny equal rho^k.
-// Distances are formed from the FP64 coordinates and then rounded to R.
+// FP64: distances formed from the coordinates.  FP32: distances formed in
+// FP32 from the point's two spacings, each rounded once from FP64.
 template <typename R>
 struct K1D
 {
