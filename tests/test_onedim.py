@@ -89,12 +89,15 @@ def test_fine_interface_equals_march_alpha2():
     del ShockTube
 
 
-def _gpu_sod(n, steps, alpha=2, precision="fp64"):
+def _gpu_sod(n, steps, alpha=2, precision="fp64", stretched=False):
     from solvcon_gb300.onedim import Euler1DCore
-    g = golden("e1d_sod") if n == 201 else None
-    dt = float(g["dt"]) if g is not None else 2 * 0.8 * (2.0 / (n - 1)) / 2.19
-    c = Euler1DCore(n, dt, precision=precision)
+    g = golden("e1d_sod") if n == 201 and not stretched else None
     x = np.linspace(-1, 1, n)
+    if stretched:  # finest at the diaphragm, 4x coarser at the ends
+        x = np.sinh(2.0947 * x) / np.sinh(2.0947)
+    dt = float(g["dt"]) if g is not None else \
+        2 * 0.8 * float(np.diff(x).min()) / 2.19
+    c = Euler1DCore(n, dt, precision=precision)
     so0 = np.zeros((n, 3))
     left = x < 0.0
     so0[:, 0] = np.where(left, 1.0, 0.125)
@@ -181,6 +184,49 @@ def test_fp32_tube_against_fp64(n, steps):
     twin.update_cfl(odd_plane=False)  # pushes so0, reads it, keeps it
     np.testing.assert_array_equal(np.array(twin.so0[...]),
                                   (so0 * (1 + 1e-12)).astype("float32"))
+
+
+@pytest.mark.gpu
+def test_fp32_tube_stretched_grid_and_clone():
+    """FP32 state on a non-uniform grid (the spacing tables are formed from
+    the coordinates written after construction) against FP64: relative L1
+    per variable <= 1e-5; a clone carries the spacing and marches on to the
+    same bits as the original."""
+    c32, x, so0, dt = _gpu_sod(2001, 300, precision="fp32", stretched=True)
+    c64, _, _, _ = _gpu_sod(2001, 300, stretched=True)
+    a = np.array(c32.so0.ndarray)
+    b = np.array(c64.so0.ndarray)
+    for k in range(3):
+        l1 = np.abs(a[:, k] - b[:, k]).sum() / np.abs(b[:, k]).sum()
+        assert l1 < 1e-5, (k, l1)
+    twin = c32.clone()
+    c32.march_alpha2(20)
+    twin.march_alpha2(20)
+    for name in ("so0", "so1", "cfl"):
+        np.testing.assert_array_equal(np.array(getattr(twin, name).ndarray),
+                                      np.array(getattr(c32, name).ndarray),
+                                      err_msg=name)
+    # A coordinate write rebuilds the spacing: a uniform grid written into
+    # the stretched core marches as a core built uniform from the start.
+    u32, xu, so0u, dtu = _gpu_sod(2001, 0, precision="fp32")
+    re = c32.clone()
+    re.coord[...] = xu
+    re.so0[...] = so0u
+    re.so1.fill(0)
+    re.cfl.fill(0)
+    re.setup_march()
+    from solvcon_gb300.onedim import Euler1DCore
+    fresh = Euler1DCore(2001, c32.time_increment, precision="fp32")
+    fresh.coord[...] = xu
+    fresh.so0[...] = so0u
+    fresh.so1.fill(0)
+    fresh.gamma.fill(1.4)
+    fresh.cfl.fill(0)
+    fresh.setup_march()
+    re.march_alpha2(50)
+    fresh.march_alpha2(50)
+    np.testing.assert_array_equal(np.array(re.so0.ndarray),
+                                  np.array(fresh.so0.ndarray))
 
 
 def test_tube_precision_must_be_known():
