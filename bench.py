@@ -218,8 +218,11 @@ def time_resident(core, steps):
 def time_e2e(core, steps):
     """K steps through the C ABI with host state: per step the state (so0n,
     so1n) is copied from pinned host memory, one march step runs, and the new
-    state is read back into the same pinned buffers.  Wall time around the
-    whole loop."""
+    state comes back into the same pinned buffers.  The buffers are
+    registered once with scg_euler_deliver, so the march's last substep
+    writes the new state over the host link as it computes it; the step ends
+    when scg_euler_sync returns with the state in host memory.  Wall time
+    around the whole loop."""
     from solvcon_gb300._lib import check, lib
     ids = {"so0n": 5, "so1n": 8}
     bufs = {}
@@ -234,6 +237,9 @@ def time_e2e(core, steps):
     h2d = bufs["so0n"][1].nbytes + bufs["so1n"][1].nbytes
     d2h = h2d
     h = core.handle
+    for name in ("so0n", "so1n"):
+        p, view = bufs[name]
+        check(lib.scg_euler_deliver(h, ids[name], p, view.size))
     core.sync()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -241,10 +247,10 @@ def time_e2e(core, steps):
             p, view = bufs[name]
             check(lib.scg_euler_set(h, ids[name], p, view.size))
         check(lib.scg_euler_march(h, 1))
-        for name in ("so0n", "so1n"):
-            p, view = bufs[name]
-            check(lib.scg_euler_get(h, ids[name], p, view.size))
+        check(lib.scg_euler_sync(h))
     t1 = time.perf_counter()
+    for name in ("so0n", "so1n"):
+        check(lib.scg_euler_deliver(h, ids[name], None, 0))
     for p, _ in bufs.values():
         check(lib.scg_host_free(p))
     return (t1 - t0) * 1e3, h2d, d2h

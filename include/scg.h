@@ -198,6 +198,19 @@ int scg_euler_op(scg_euler * core, int op);
  * scg_euler_sync waits for it. */
 int scg_euler_march(scg_euler * core, int64_t steps);
 int scg_euler_sync(scg_euler * core);
+/* Not in the reference: have every later march also leave array `which`
+ * (SCG_EA_SO0N or SCG_EA_SO1N, the whole array of `count` doubles in the
+ * layout scg_euler_get gives) in the host block `host`, written by the last
+ * substep's kernel as it computes, so the result crosses the host link while
+ * the march runs instead of in a copy after it.  After scg_euler_sync (or
+ * any synchronous call) the block holds what scg_euler_get would return.
+ * host must be a 16-byte aligned range of one scg_host_alloc block; NULL
+ * stops the delivery.  A block freed while registered is dropped at the next
+ * march and never written.  The replacement for the reference's pattern of
+ * march(steps) followed by reading so0n / so1n (euler_march.cpp:350-359;
+ * the so0n / so1n properties, multidim/pymod/wrap_multidim.cpp:393-396)
+ * when the host reads every step. */
+int scg_euler_deliver(scg_euler * core, int which, double * host, int64_t count);
 /* Run the core on a caller-owned cudaStream_t (null restores its own). */
 int scg_euler_set_stream(scg_euler * core, void * cuda_stream);
 /* W-3/4 limiter firing bits of the last calc_dsoln per body cell: bit i set

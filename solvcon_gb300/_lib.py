@@ -69,6 +69,8 @@ _SIGS = {
     "scg_euler_op": ([_vp, ctypes.c_int], ctypes.c_int),
     "scg_euler_march": ([_vp, ctypes.c_int64], ctypes.c_int),
     "scg_euler_sync": ([_vp], ctypes.c_int),
+    "scg_euler_deliver": ([_vp, ctypes.c_int, _vp, ctypes.c_int64],
+                          ctypes.c_int),
     "scg_euler_set_stream": ([_vp, _vp], ctypes.c_int),
     "scg_euler_limiter_mask": ([_vp, _vp], ctypes.c_int),
     "scg_euler_totals": ([_vp, _vp], ctypes.c_int),

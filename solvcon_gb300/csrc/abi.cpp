@@ -338,6 +338,11 @@ int scg_euler_march(scg_euler * core, int64_t steps)
     });
 }
 
+int scg_euler_deliver(scg_euler * core, int which, double * host, int64_t count)
+{
+    return guarded([&] { need(core, "scg_euler_deliver")->c->deliver(which, host, count); });
+}
+
 int scg_euler_sync(scg_euler * core)
 {
     return guarded([&] { need(core, "scg_euler_sync")->c->sync(); });

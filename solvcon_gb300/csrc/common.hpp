@@ -41,8 +41,10 @@ extern std::atomic<int64_t> g_launches;
 // The device address of the host range [p, p + nbytes) when the whole range
 // lies inside one block from scg_host_alloc (page-locked and mapped into the
 // device's address space), else nullptr.  Kernels may then load and store
-// the range directly over the host link, with no staging copy.
-void * mapped_host(void const * p, size_t nbytes);
+// the range directly over the host link, with no staging copy.  With serial
+// set it also receives the block's allocation number, which differs between
+// two blocks that happen to reuse one address.
+void * mapped_host(void const * p, size_t nbytes, uint64_t * serial = nullptr);
 
 inline void cuda_check(cudaError_t rc, char const * what)
 {

@@ -1029,6 +1029,8 @@ public:
         a.gnml = d_gnml.ptr;
         a.gval = d_gval.ptr;
         a.limiter = d_limiter.ptr;
+        a.out0 = m_deliver_now ? m_deliver[0].dev : nullptr;
+        a.out1 = m_deliver_now ? m_deliver[1].dev : nullptr;
         a.ncell = ncell;
         a.ngst = ngstcell;
         a.dt = R(time_increment);
@@ -1366,12 +1368,43 @@ public:
     void march(int64_t steps) override
     {
         upload_bc();
+        bool const delivers = steps > 0 && revalidate_delivery();
         for (int64_t s = 0; s < steps; ++s)
         {
             march_substep();
+            m_deliver_now = delivers && s + 1 == steps;
             march_substep();
+            m_deliver_now = false;
         }
         async_pending = steps > 0 && nrow > 0;
+    }
+
+    void deliver(int which, double * host, int64_t count) override
+    {
+        if (which != EA_SO0N && which != EA_SO1N)
+        {
+            throw std::invalid_argument("EulerCore.deliver: only so0n and so1n are delivered");
+        }
+        Delivery & d = m_deliver[which == EA_SO0N ? 0 : 1];
+        if (!host)
+        {
+            d = Delivery{};
+            return;
+        }
+        if (count != array_size(which))
+        {
+            throw std::invalid_argument("EulerCore.deliver: count " + std::to_string(count) + " is not the array's " +
+                                        std::to_string(array_size(which)));
+        }
+        size_t const nb = static_cast<size_t>(count) * sizeof(double);
+        uint64_t serial = 0;
+        void * const dev = mapped_host(host, nb, &serial);
+        if (!dev || reinterpret_cast<uintptr_t>(dev) % 16 != 0)
+        {
+            throw std::invalid_argument("EulerCore.deliver: host must be a 16-byte aligned range of one "
+                                        "scg_host_alloc block");
+        }
+        d = Delivery{host, static_cast<double *>(dev), nb, serial};
     }
 
     void limiter_mask(uint8_t * out) override
@@ -1558,6 +1591,40 @@ private:
     DevBuf<int8_t> d_ctype;
     DevBuf<R> rec[2];
     DevBuf<R> d_gamma, d_cflo, d_cflc;
+
+    // Host blocks a march also writes so0n / so1n into (deliver()).
+    struct Delivery
+    {
+        double * host = nullptr;
+        double * dev = nullptr;
+        size_t nbytes = 0;
+        uint64_t serial = 0;
+    };
+    Delivery m_deliver[2];
+    bool m_deliver_now = false;
+
+    // True when a delivery is registered; a block freed since registration
+    // (or a new block at its address) is dropped, never written.
+    bool revalidate_delivery()
+    {
+        bool any = false;
+        for (Delivery & d : m_deliver)
+        {
+            if (!d.host)
+            {
+                continue;
+            }
+            uint64_t serial = 0;
+            void * const dev = mapped_host(d.host, d.nbytes, &serial);
+            if (dev != d.dev || serial != d.serial)
+            {
+                d = Delivery{};
+                continue;
+            }
+            any = true;
+        }
+        return any;
+    }
     DevBuf<uint8_t> d_limiter;
     DevBuf<int8_t> d_gkind;
     DevBuf<double> d_gnml, d_gval;

@@ -114,6 +114,11 @@ public:
     virtual void init_solution(double gamma, double rho, double const * v, double p) = 0;
     virtual void op(int which) = 0;
     virtual void march(int64_t steps) = 0;
+    // Have every later march also leave array `which` (EA_SO0N or EA_SO1N)
+    // of its last substep in the host block `host` (a whole-array, 16-byte
+    // aligned range of one scg_host_alloc block), written by the march kernel
+    // itself; host = nullptr stops it.
+    virtual void deliver(int which, double * host, int64_t count) = 0;
     virtual void sync() = 0;
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void limiter_mask(uint8_t * out) = 0;

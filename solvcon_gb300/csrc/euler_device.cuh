@@ -394,6 +394,10 @@ struct MarchArgs
     double const * gnml;  // [ngst][ND] outward unit normal of the boundary face
     double const * gval;  // [ngst][NEQ] inlet conserved state
     uint8_t * limiter;    // [ncell] W-3/4 firing bits per equation, or null
+    // Host blocks (mapped) that also receive every row's new so0n
+    // [nrow][NEQ] and so1n [nrow][NEQ][ND] in FP64, or null.
+    double * out0;
+    double * out1;
     int64_t ncell;
     int64_t ngst;
     R dt, hdt, qdt;

@@ -876,6 +876,55 @@ __device__ __forceinline__ void bc1_ghost(int kind, double const * n, R const * 
     }
 }
 
+// A row's new so0n and so1n, as FP64, into the host blocks of a march that
+// delivers them (out0, out1), in the layout of the host arrays: the bytes
+// leave over the host link while the march still computes.
+template <int ND, typename R, typename G>
+__device__ __forceinline__ void deliver_row(MarchArgs<R, G> const & a, int64_t row, R const * so0, R const * so1)
+{
+    constexpr int NEQ = ND + 2;
+    if (a.out0)
+    {
+        double * const o = a.out0 + row * NEQ;
+        if constexpr (NEQ % 2 == 0)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; i += 2)
+            {
+                *reinterpret_cast<double2 *>(o + i) = make_double2(double(so0[i]), double(so0[i + 1]));
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                o[i] = double(so0[i]);
+            }
+        }
+    }
+    if (a.out1)
+    {
+        double * const o = a.out1 + row * (NEQ * ND);
+        if constexpr ((NEQ * ND) % 2 == 0)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ * ND; i += 2)
+            {
+                *reinterpret_cast<double2 *>(o + i) = make_double2(double(so1[i]), double(so1[i + 1]));
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ * ND; ++i)
+            {
+                o[i] = double(so1[i]);
+            }
+        }
+    }
+}
+
 // One fused CESE substep for one body cell: soln, bc_soln of its boundary
 // faces, cfl, dsoln, bc_dsoln of its boundary faces, and calc_solt of the next
 // substep for its own row and its ghost rows.  Reads only the current records
@@ -928,6 +977,7 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
                 Prim<ND, R> const qg(g0, ldg(a.gamma + jr));
                 solt_prim<ND, R>(qg, g0, g1, gt);
                 store_rec<ND, R>(a.nxt + jr * Rec<ND, R>::RS, g0, gt, g1, qg);
+                deliver_row<ND>(a, jr, g0, g1);
             }
         }
     }
@@ -959,6 +1009,7 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     Prim<ND, R> const q(so0n, ldg(a.gamma + row), rinv);
     solt_prim<ND, R>(q, so0n, so1n, so0t);
     store_rec<ND, R>(a.nxt + row * Rec<ND, R>::RS, so0n, so0t, so1n, q);
+    deliver_row<ND>(a, row, so0n, so1n);
 }
 
 // The work of thread t of one substep: body cell t for t < ncell, ghost row
@@ -1008,6 +1059,7 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
             Prim<ND, R> const q(rec, ldg(a.gamma + g));
             solt_prim<ND, R>(q, rec, rec + 2 * NEQ, tt);
             store_rec<ND, R>(a.nxt + g * Rec<ND, R>::RS, rec, tt, rec + 2 * NEQ, q);
+            deliver_row<ND>(a, g, rec, rec + 2 * NEQ);
         }
     }
 }

@@ -21,13 +21,15 @@ struct HostBlock
 {
     size_t nbytes;
     void * dev;
+    uint64_t serial; // distinct for every allocation, reused addresses included
 };
 std::mutex g_blocks_mutex;
 std::map<uintptr_t, HostBlock> g_blocks;
+uint64_t g_block_serial = 0;
 
 } // namespace
 
-void * scg::mapped_host(void const * p, size_t nbytes)
+void * scg::mapped_host(void const * p, size_t nbytes, uint64_t * serial)
 {
     uintptr_t const a = reinterpret_cast<uintptr_t>(p);
     std::lock_guard<std::mutex> lk(g_blocks_mutex);
@@ -42,6 +44,10 @@ void * scg::mapped_host(void const * p, size_t nbytes)
     if (!b.dev || off > b.nbytes || nbytes > b.nbytes - off)
     {
         return nullptr;
+    }
+    if (serial)
+    {
+        *serial = b.serial;
     }
     return static_cast<char *>(b.dev) + off;
 }
@@ -145,7 +151,7 @@ int scg_host_alloc(int64_t nbytes, void ** out)
         }
         {
             std::lock_guard<std::mutex> lk(g_blocks_mutex);
-            g_blocks[reinterpret_cast<uintptr_t>(p)] = {static_cast<size_t>(nbytes), d};
+            g_blocks[reinterpret_cast<uintptr_t>(p)] = {static_cast<size_t>(nbytes), d, ++g_block_serial};
         }
         *out = p;
     });

@@ -157,3 +157,95 @@ def test_mapped_so1n_after_update_keeps_so0t(precision):
     b.march(1)
     np.testing.assert_array_equal(_get(b, 5, _shape(b, "so0n")),
                                   _get(a, 5, _shape(a, "so0n")))
+
+
+def _delivery_core(precision, kind):
+    """A marched core: triangles or tetrahedra (the simplex kernels), quads
+    (the generic kernel), or triangles with slip walls on half of the
+    boundary faces (ghost rows without a condition)."""
+    import solvcon_gb300 as sg
+    from solvcon_gb300 import meshgen
+    if kind == "tet":
+        return _marched_core(precision, 3)
+    if kind == "tri":
+        return _marched_core(precision, 2)
+    if kind == "quad":
+        x, t, c = meshgen.quad_square(12, 0.15, 2)
+    else:
+        x, t, c = meshgen.tri_square(16, 0.2, 4)
+    mesh = meshgen.build_mesh(2, x, t, c)
+    ec = sg.EulerCore(mesh=mesh, time_increment=2e-3, precision=precision)
+    clcnd = np.array(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    faces = [int(f) for f in mesh.bndfcs.ndarray[:, 0]]
+    ec.add_slipwall(faces if kind == "quad" else faces[::2])
+    meshgen.set_state(ec, mesh, meshgen.quadrant_state(clcnd, seed=7), 1.4)
+    ec.march(2)
+    ec.release_views()
+    return ec
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("kind", ["tri", "tet", "quad", "partial_bc"])
+def test_march_delivers_so0n_so1n(precision, kind):
+    """scg_euler_deliver: a march leaves so0n and so1n of its last substep
+    in the registered host blocks, every row (ghost rows with and without a
+    boundary condition included) equal bit for bit to scg_euler_get; the
+    blocks are written only by marches, and no longer once deregistered."""
+    from solvcon_gb300._lib import check, lib
+    ec = _delivery_core(precision, kind)
+    h = ec.handle
+    blocks = {}
+    try:
+        for name in ("so0n", "so1n"):
+            shape = _shape(ec, name)
+            blk = _Block(int(np.prod(shape)))
+            blk.view[...] = np.nan
+            check(lib.scg_euler_deliver(h, RECORD_TABLES[name],
+                                        ctypes.c_void_p(blk.addr),
+                                        blk.view.size))
+            blocks[name] = (blk, shape)
+        for steps in (1, 3):
+            check(lib.scg_euler_march(h, steps))
+            check(lib.scg_euler_sync(h))
+            for name, (blk, shape) in blocks.items():
+                np.testing.assert_array_equal(
+                    blk.view.reshape(shape),
+                    _get(ec, RECORD_TABLES[name], shape), err_msg=name)
+        # Operations other than march leave the blocks alone.
+        for blk, _ in blocks.values():
+            blk.view[...] = np.nan
+        ec.calc_soln()
+        ec.release_views()
+        for blk, _ in blocks.values():
+            assert np.isnan(blk.view).all()
+        for name in blocks:
+            check(lib.scg_euler_deliver(h, RECORD_TABLES[name], None, 0))
+        check(lib.scg_euler_march(h, 1))
+        check(lib.scg_euler_sync(h))
+        for blk, _ in blocks.values():
+            assert np.isnan(blk.view).all()
+    finally:
+        for blk, _ in blocks.values():
+            blk.free()
+
+
+def test_deliver_rejects_bad_targets():
+    from solvcon_gb300._lib import check, lib, ptr
+    ec = _marched_core("fp64", 2)
+    h = ec.handle
+    n0 = int(np.prod(_shape(ec, "so0n")))
+    pageable = np.zeros(n0)
+    with pytest.raises(ValueError):  # not a mapped block
+        check(lib.scg_euler_deliver(h, 5, ptr(pageable), n0))
+    blk = _Block(n0 + 1, skip=1)
+    try:
+        with pytest.raises(ValueError):  # only 8-byte aligned
+            check(lib.scg_euler_deliver(h, 5, ctypes.c_void_p(blk.addr), n0))
+        with pytest.raises(ValueError):  # not the array's size
+            check(lib.scg_euler_deliver(h, 5, ctypes.c_void_p(blk.ptr.value),
+                                        n0 - 1))
+        with pytest.raises(ValueError):  # so0c is not delivered
+            check(lib.scg_euler_deliver(h, 4, ctypes.c_void_p(blk.ptr.value),
+                                        n0))
+    finally:
+        blk.free()

@@ -52,18 +52,27 @@ def test_results_same_alone_and_in_the_mix():
         assert r.latency >= 0 and r.t_admit >= r.arrival - 1e-9
 
 
+def _jump_clock():
+    """A clock that advances one second per reading: every request has
+    arrived by the first tick, so admission depends on the budget alone and
+    not on how fast the device runs."""
+    import itertools
+    return itertools.count(0.0, 1.0).__next__
+
+
 def test_budget_limits_resident_set():
     from solvcon_gb300.serving import alone
     budget = 1200000
     srv = _server(budget=budget, max_chunk=8)
     reqs = _requests()
-    done = srv.run(reqs)
+    done = srv.run(reqs, clock=_jump_clock())
     assert len(done) + len(srv.rejected) == len(reqs)
     assert not srv.rejected
     assert srv.peak_held <= budget
     big = _server(budget=1 << 34, max_chunk=8)
-    big.run(_requests())
-    assert srv.peak_resident <= big.peak_resident
+    big.run(_requests(), clock=_jump_clock())
+    assert big.peak_resident == len(reqs)
+    assert 1 <= srv.peak_resident <= big.peak_resident
     for r in done:
         ref, _ = alone(srv, r, "fp32")
         np.testing.assert_array_equal(r.result, ref, "request %d" % r.rid)
