@@ -219,10 +219,11 @@ def time_e2e(core, steps):
     """K steps through the C ABI with host state: per step the state (so0n,
     so1n) is copied from pinned host memory, one march step runs, and the new
     state comes back into the same pinned buffers.  The buffers are
-    registered once with scg_euler_deliver, so the march's last substep
-    writes the new state over the host link as it computes it; the step ends
-    when scg_euler_sync returns with the state in host memory.  Wall time
-    around the whole loop."""
+    registered once with scg_euler_deliver: an FP64 march's last substep
+    writes the new state over the host link as it computes it, an FP32
+    march queues a coalesced gather into them after it; the step ends when
+    scg_euler_sync returns with the state in host memory.  Wall time around
+    the whole loop."""
     from solvcon_gb300._lib import check, lib
     ids = {"so0n": 5, "so1n": 8}
     bufs = {}

@@ -200,9 +200,12 @@ int scg_euler_march(scg_euler * core, int64_t steps);
 int scg_euler_sync(scg_euler * core);
 /* Not in the reference: have every later march also leave array `which`
  * (SCG_EA_SO0N or SCG_EA_SO1N, the whole array of `count` doubles in the
- * layout scg_euler_get gives) in the host block `host`, written by the last
- * substep's kernel as it computes, so the result crosses the host link while
- * the march runs instead of in a copy after it.  After scg_euler_sync (or
+ * layout scg_euler_get gives) in the host block `host`.  An FP64 core's last
+ * substep kernel writes the rows as it computes them, so the result crosses
+ * the host link while the FP64-bound march runs instead of in a copy after
+ * it; an FP32 core (latency-bound, its scattered row stores would not fill
+ * whole lines) queues a coalesced gather into the block right after the
+ * march.  After scg_euler_sync (or
  * any synchronous call) the block holds what scg_euler_get would return.
  * host must be a 16-byte aligned range of one scg_host_alloc block; NULL
  * stops the delivery.  A block freed while registered is dropped at the next

@@ -1368,13 +1368,35 @@ public:
     void march(int64_t steps) override
     {
         upload_bc();
-        bool const delivers = steps > 0 && revalidate_delivery();
+        // FP64: the last substep's kernel writes the rows itself, hidden
+        // under its FP64 arithmetic.  FP32: the march is bound by load
+        // latency and its per-row host stores would not coalesce into whole
+        // lines, so the delivery is a coalesced gather queued after it.
+        bool const delivers = steps > 0 && nrow > 0 && revalidate_delivery();
+        constexpr bool IN_KERNEL = sizeof(R) == 8;
         for (int64_t s = 0; s < steps; ++s)
         {
             march_substep();
-            m_deliver_now = delivers && s + 1 == steps;
+            m_deliver_now = IN_KERNEL && delivers && s + 1 == steps;
             march_substep();
             m_deliver_now = false;
+        }
+        if (!IN_KERNEL && delivers)
+        {
+            for (int k = 0; k < 2; ++k)
+            {
+                Delivery const & d = m_deliver[k];
+                if (d.host)
+                {
+                    R * base;
+                    int off, width;
+                    field_of(k == 0 ? EA_SO0N : EA_SO1N, base, off, width);
+                    int64_t const n = static_cast<int64_t>(d.nbytes / sizeof(double));
+                    k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(base, d.dev, nrow, off,
+                                                                                       width, true);
+                    launched(stream, "get_field_host");
+                }
+            }
         }
         async_pending = steps > 0 && nrow > 0;
     }

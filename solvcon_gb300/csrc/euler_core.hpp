@@ -116,8 +116,9 @@ public:
     virtual void march(int64_t steps) = 0;
     // Have every later march also leave array `which` (EA_SO0N or EA_SO1N)
     // of its last substep in the host block `host` (a whole-array, 16-byte
-    // aligned range of one scg_host_alloc block), written by the march kernel
-    // itself; host = nullptr stops it.
+    // aligned range of one scg_host_alloc block): written by the last FP64
+    // substep kernel itself, or by a gather queued after an FP32 march;
+    // host = nullptr stops it.
     virtual void deliver(int which, double * host, int64_t count) = 0;
     virtual void sync() = 0;
     virtual void set_stream(cudaStream_t s) = 0;
