@@ -209,7 +209,8 @@ int scg_euler_sync(scg_euler * core);
  * any synchronous call) the block holds what scg_euler_get would return.
  * host must be a 16-byte aligned range of one scg_host_alloc block; NULL
  * stops the delivery.  A block freed while registered is dropped at the next
- * march and never written.  The replacement for the reference's pattern of
+ * march and never written; free a block only after scg_euler_sync, since an
+ * asynchronous march may still be writing it.  The replacement for the reference's pattern of
  * march(steps) followed by reading so0n / so1n (euler_march.cpp:350-359;
  * the so0n / so1n properties, multidim/pymod/wrap_multidim.cpp:393-396)
  * when the host reads every step. */
