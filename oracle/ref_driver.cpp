@@ -16,6 +16,8 @@
 #include <solvcon/mesh/mesh.hpp>
 #include <solvcon/multidim/multidim.hpp>
 #include <solvcon/onedim/Euler1DCore.hpp>
+#include <solvcon/spacetime/kernel/inviscid_burgers.hpp>
+#include <solvcon/spacetime/kernel/linear_scalar.hpp>
 
 #include <cstring>
 #include <memory>
@@ -27,6 +29,7 @@ using solvcon::EulerCore;
 using solvcon::SimpleArray;
 using solvcon::StaticMesh;
 using solvcon::onedim::Euler1DCore;
+namespace st = solvcon::spacetime;
 
 namespace
 {
@@ -46,6 +49,22 @@ struct RefEuler
 struct RefEuler1D
 {
     std::shared_ptr<Euler1DCore> core;
+};
+
+// One of the reference's spacetime scalar solvers: kind 0 LinearScalarSolver,
+// kind 1 InviscidBurgersSolver.
+struct RefSpacetime
+{
+    int kind = 0;
+    std::shared_ptr<st::LinearScalarSolver> linear;
+    std::shared_ptr<st::InviscidBurgersSolver> burgers;
+
+    template <typename F>
+    void visit(F && f)
+    {
+        if (kind == 0) f(*linear);
+        else f(*burgers);
+    }
 };
 
 template <typename F>
@@ -313,6 +332,65 @@ int ref_e1d_march(void * h, int op, int steps)
         else if (op == 1) c.march_alpha<1>(static_cast<size_t>(steps));
         else if (op == 2) c.march_alpha<2>(static_cast<size_t>(steps));
         else throw std::invalid_argument("bad op"); });
+}
+
+// ---- spacetime solvers ----------------------------------------------------
+
+// Grid::construct(xloc) (the CE boundaries, ascending) and the solver of the
+// given kind on it (kernel/linear_scalar.hpp:32-42, kernel/inviscid_burgers.hpp:30-45).
+int ref_st_create(int kind, double const * xloc, long long nloc, double dt, void ** out)
+{
+    return guard([&]
+                 {
+        if (kind != 0 && kind != 1) throw std::invalid_argument("bad solver kind");
+        st::Grid::array_type loc(solvcon::small_vector<ssize_t>{static_cast<ssize_t>(nloc)});
+        for (long long i = 0; i < nloc; ++i) loc[i] = xloc[i];
+        auto grid = st::Grid::construct(loc);
+        auto * h = new RefSpacetime;
+        h->kind = kind;
+        if (kind == 0) h->linear = st::LinearScalarSolver::construct(grid, dt);
+        else h->burgers = st::InviscidBurgersSolver::construct(grid, dt);
+        *out = h; });
+}
+
+void ref_st_destroy(void * h) { delete static_cast<RefSpacetime *>(h); }
+
+// which: 0 xcoord, 1 so0, 2 so1, 3 cfl (whole tables, nvar = 1).  *count
+// receives the table's element count; out / in may be null.
+int ref_st_array(void * h, int which, double * out, double const * in, long long * count)
+{
+    return guard([&]
+                 {
+        static_cast<RefSpacetime *>(h)->visit([&](auto & s)
+        {
+            SimpleArray<double> * a = nullptr;
+            switch (which)
+            {
+            case 0: a = &s.grid().xcoord(); break;
+            case 1: a = &s.so0(); break;
+            case 2: a = &s.so1(); break;
+            case 3: a = &s.cfl(); break;
+            default: throw std::invalid_argument("bad array");
+            }
+            *count = static_cast<long long>(a->size());
+            if (in) copy_in(*a, in);
+            if (out) copy_out(*a, out);
+        }); });
+}
+
+// op: 0 setup_march, 1 march_alpha<1>(steps), 2 march_alpha<2>(steps)
+// (core.hpp:804-810, 1029-1036).
+int ref_st_march(void * h, int op, long long steps)
+{
+    return guard([&]
+                 {
+        static_cast<RefSpacetime *>(h)->visit([&](auto & s)
+        {
+            if (op == 0) s.setup_march();
+            else if (op == 1) s.template march_alpha<1>(static_cast<size_t>(steps));
+            else if (op == 2) s.template march_alpha<2>(static_cast<size_t>(steps));
+            else throw std::invalid_argument("bad op");
+        }); });
 }
 
 } // extern "C"

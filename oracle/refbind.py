@@ -226,3 +226,54 @@ class RefEuler1D:
         if getattr(self, "h", None) is not None and _lib is not None:
             _lib.ref_e1d_destroy(self.h)
             self.h = None
+
+
+class RefSpacetime:
+    """The reference spacetime LinearScalarSolver (kind 0) or
+    InviscidBurgersSolver (kind 1) on a Grid built from the CE boundaries
+    ``xloc``; tables are whole [2 ncelm + 5] arrays (nvar = 1)."""
+
+    NAMES = {"xcoord": 0, "so0": 1, "so1": 2, "cfl": 3}
+
+    def __init__(self, kind, xloc, time_increment):
+        xloc = np.ascontiguousarray(xloc, dtype="float64")
+        h = ctypes.c_void_p()
+        lib().ref_st_create.argtypes = [ctypes.c_int, ctypes.c_void_p,
+                                        ctypes.c_longlong, ctypes.c_double,
+                                        ctypes.c_void_p]
+        lib().ref_st_array.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+        lib().ref_st_march.argtypes = [ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_longlong]
+        _check(lib().ref_st_create(kind, _dp(xloc), xloc.size,
+                                   time_increment, ctypes.byref(h)))
+        self.h = h
+        cnt = ctypes.c_longlong()
+        _check(lib().ref_st_array(h, 0, None, None, ctypes.byref(cnt)))
+        self.xsize = cnt.value
+
+    def get(self, name):
+        out = np.empty(self.xsize, dtype="float64")
+        cnt = ctypes.c_longlong()
+        _check(lib().ref_st_array(self.h, self.NAMES[name], _dp(out), None,
+                                  ctypes.byref(cnt)))
+        return out
+
+    def set(self, name, value):
+        arr = np.ascontiguousarray(value, dtype="float64").reshape(
+            self.xsize)
+        cnt = ctypes.c_longlong()
+        _check(lib().ref_st_array(self.h, self.NAMES[name], None, _dp(arr),
+                                  ctypes.byref(cnt)))
+
+    def setup_march(self):
+        _check(lib().ref_st_march(self.h, 0, 0))
+
+    def march_alpha(self, alpha, steps):
+        _check(lib().ref_st_march(self.h, alpha, steps))
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.ref_st_destroy(self.h)
+            self.h = None

@@ -12,10 +12,13 @@ seeded cases and stores its outputs as .npz files:
 * gmsh_<case>.npz -- a Gmsh MSH 2.2 file written by meshgen.to_gmsh (its text
   in "msh") and every StaticMesh table the reference's Gmsh reader builds
   from it;
-* plot3d_<case>.npz -- the same for Plot3D grid files (text in "p3d").
+* plot3d_<case>.npz -- the same for Plot3D grid files (text in "p3d");
+* st_<solver>_a<alpha>.npz -- a spacetime LinearScalarSolver /
+  InviscidBurgersSolver on a non-uniform grid: its CE boundaries, dt, the
+  initial so0/so1 and the so0/so1/cfl tables after march_alpha<alpha>.
 
-Usage: python tests/golden/make_golden.py [gmsh]   (needs oracle/_ref built;
-"gmsh" / "plot3d" write only that reader's fixtures)
+Usage: python tests/golden/make_golden.py [gmsh|plot3d|spacetime]   (needs
+oracle/_ref built; a mode argument writes only those fixtures)
 """
 
 import os
@@ -126,6 +129,48 @@ def e1d_golden():
     np.savez_compressed(os.path.join(HERE, "e1d_sod.npz"), **out)
 
 
+def spacetime_cases():
+    """Spacetime solver cases on non-uniform grids (CE boundaries jittered
+    by up to 30% of the mean spacing, seeded): the linear scalar advecting
+    sin(x) (so1 = cos(x)), and inviscid Burgers from u = 0.5 + sin(x), which
+    steepens into a shock at t = 1 and is marched to t ~ 2.  dt gives a CFL
+    number of 0.9 on the smallest half spacing at the largest speed.  Returns
+    {name: (kind, alpha, xloc, dt, steps, so0 at CE boundaries / centres,
+    so1)} with so0/so1 given as functions of the grid's coordinates."""
+    out = {}
+    for name, kind, ncelm, umax, steps in (("linear", 0, 80, 1.0, 60),
+                                           ("burgers", 1, 200, 1.5, 240)):
+        rng = np.random.Generator(np.random.PCG64(4242 + kind))
+        h = 2 * np.pi / ncelm
+        xloc = np.arange(ncelm + 1) * h
+        xloc[1:-1] += rng.uniform(-0.3, 0.3, ncelm - 1) * h
+        hmin = np.diff(xloc).min() / 2
+        dt = 0.9 * 2 * hmin / umax
+        for alpha in (1, 2):
+            out["%s_a%d" % (name, alpha)] = (kind, alpha, xloc, dt, steps)
+    return out
+
+
+def spacetime_golden(name, kind, alpha, xloc, dt, steps):
+    s = rb.RefSpacetime(kind, xloc, dt)
+    x = s.get("xcoord")
+    so0 = np.sin(x) + (0.5 if kind == 1 else 0.0)
+    so1 = np.cos(x)
+    s.set("so0", so0)
+    s.set("so1", so1)
+    # The two outermost entries of cfl are never written by the solver
+    # (core.hpp:954-962 covers selms -1 .. nselm-1 only); start from zeros so
+    # the fixture holds no uninitialised memory.
+    s.set("cfl", np.zeros_like(x))
+    s.setup_march()
+    out = {"kind": kind, "alpha": alpha, "xloc": xloc, "dt": dt,
+           "steps": steps, "xcoord": x, "so0_in": so0, "so1_in": so1}
+    s.march_alpha(alpha, steps)
+    for a in ("so0", "so1", "cfl"):
+        out[a] = s.get(a)
+    np.savez_compressed(os.path.join(HERE, "st_%s.npz" % name), **out)
+
+
 def gmsh_cases():
     """Gmsh files of the reader's fixtures: (text, ndim, ndcrd, cltpn, clnds)
     where the last three are the mesh the file describes (None when the file
@@ -233,6 +278,11 @@ def main():
             gmsh_golden(name, case[0])
         print("gmsh fixtures written to", HERE)
         return
+    if sys.argv[1:] == ["spacetime"]:
+        for name, case in spacetime_cases().items():
+            spacetime_golden(name, *case)
+        print("spacetime fixtures written to", HERE)
+        return
     if sys.argv[1:] == ["plot3d"]:
         for name, text in plot3d_cases().items():
             mesh_golden_from("plot3d_" + name,
@@ -251,6 +301,8 @@ def main():
                                      radius=0.35)
         march_golden(name, mesh, nd, state, kind, 2e-3, 6)
     e1d_golden()
+    for name, case in spacetime_cases().items():
+        spacetime_golden(name, *case)
     for name, case in gmsh_cases().items():
         gmsh_golden(name, case[0])
     for name, text in plot3d_cases().items():

@@ -153,3 +153,59 @@ def test_oracle_against_reference_library():
         o.march(3)
         for a in ("so0n", "so1n", "so0t", "cflc"):
             np.testing.assert_array_equal(getattr(o, a), ref.get(a), a)
+
+
+ST_CASES = ["linear_a1", "linear_a2", "burgers_a1", "burgers_a2"]
+
+
+@pytest.mark.parametrize("case", ST_CASES)
+def test_oracle_reproduces_reference_spacetime(case):
+    """The spacetime oracle against the reference's own solvers
+    (spacetime/core.hpp:946-1036, kernel/linear_scalar.hpp,
+    kernel/inviscid_burgers.hpp) on non-uniform grids: a linear-scalar wave
+    and a Burgers state that steepens into a shock, alpha 1 and 2
+    (fixtures generated from the reference)."""
+    from oracle import oracle as ora
+    g = golden("st_" + case)
+    o = ora.OracleSpacetime(int(g["kind"]), g["xcoord"], float(g["dt"]))
+    o.so0[:] = g["so0_in"]
+    o.so1[:] = g["so1_in"]
+    o.setup_march()
+    o.march_alpha(int(g["alpha"]), int(g["steps"]))
+    for a in ("so0", "so1", "cfl"):
+        np.testing.assert_array_equal(getattr(o, a), g[a], a)
+
+
+def test_oracle_spacetime_against_reference_library():
+    """The same comparison against the reference library live, on other
+    grids and states, marched half a step at a time and in one call."""
+    from oracle import oracle as ora
+    from oracle import refbind as rb
+    if not rb.available():
+        pytest.skip("reference library not built on this host")
+    rng = np.random.default_rng(99)
+    for kind, ncelm in ((0, 57), (1, 131)):
+        h = 3.0 / ncelm
+        xloc = -1.0 + np.arange(ncelm + 1) * h
+        xloc[1:-1] += rng.uniform(-0.35, 0.35, ncelm - 1) * h
+        dt = 0.8 * np.diff(xloc).min() / 1.6
+        for alpha in (1, 2):
+            ref = rb.RefSpacetime(kind, xloc, dt)
+            x = ref.get("xcoord")
+            so0 = np.where(x < 0.2, 1.2, -0.3) + 0.1 * np.sin(7 * x)
+            so1 = np.zeros_like(x)
+            ref.set("so0", so0)
+            ref.set("so1", so1)
+            ref.set("cfl", np.zeros_like(x))
+            o = ora.OracleSpacetime(kind, x, dt)
+            o.so0[:] = so0
+            o.so1[:] = so1
+            ref.setup_march()
+            o.setup_march()
+            for k in (1, 1, 5, 40):
+                ref.march_alpha(alpha, k)
+                o.march_alpha(alpha, k)
+                for a in ("so0", "so1", "cfl"):
+                    np.testing.assert_array_equal(getattr(o, a), ref.get(a),
+                                                  "%d %d %s" % (kind, alpha,
+                                                                a))

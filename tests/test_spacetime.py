@@ -102,3 +102,29 @@ def test_matches_oracle(cls, kind, alpha):
     assert_rel(svr.so0.ndarray[:, 0], ref.so0, 1e-12, "so0")
     assert_rel(svr.so1.ndarray[:, 0], ref.so1, 1e-10, "so1")
     assert_rel(svr.cfl.ndarray, ref.cfl, 1e-12, "cfl")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["linear_a1", "linear_a2", "burgers_a1",
+                                  "burgers_a2"])
+def test_matches_reference_golden(case):
+    """The GPU solvers against the reference's own output on a non-uniform
+    grid (fixtures made by running the reference): a linear-scalar wave, and
+    a Burgers state that has steepened into a shock."""
+    from _util import golden
+    from solvcon_gb300 import spacetime as st
+    g = golden("st_" + case)
+    grid = st.Grid(g["xloc"])
+    np.testing.assert_array_equal(grid.xcoord, g["xcoord"])
+    cls = (st.LinearScalarSolver, st.InviscidBurgersSolver)[int(g["kind"])]
+    svr = cls(grid=grid, time_increment=float(g["dt"]))
+    svr.so0.ndarray[:, 0] = g["so0_in"]
+    svr.so1.ndarray[:, 0] = g["so1_in"]
+    svr.setup_march()
+    if int(g["alpha"]) == 1:
+        svr.march_alpha1(int(g["steps"]))
+    else:
+        svr.march_alpha2(int(g["steps"]))
+    assert_rel(svr.so0.ndarray[:, 0], g["so0"], 1e-12, "so0")
+    assert_rel(svr.so1.ndarray[:, 0], g["so1"], 1e-10, "so1")
+    assert_rel(svr.cfl.ndarray, g["cfl"], 1e-12, "cfl")
