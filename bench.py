@@ -23,8 +23,10 @@ march that equals the compiled reference bit for bit: the reference library
 is built from the reference's sources, which a machine without them cannot
 do).  The line then carries that rate in ``value``, ``cpu_baseline`` and
 ``e2e``.
-Under torchrun with N > 1 every rank marches its own mesh (replicas: a single
-mesh is not decomposed), times are maxed over ranks and the value is the sum.
+With ``--gpus N`` (N > 1) every rank marches its own mesh on its own GPU
+(replicas: a single mesh is not decomposed), times are maxed over ranks and
+the value is the sum.  Launched without a launcher, the command starts its N
+ranks itself under ``torch.distributed.run`` (rendezvous on 127.0.0.1).
 """
 
 import argparse
@@ -366,6 +368,24 @@ def pin_device(local):
     devs = [d for d in seen.split(",") if d.strip()]
     if len(devs) > 1 and local < len(devs):
         os.environ["CUDA_VISIBLE_DEVICES"] = devs[local].strip()
+
+
+def free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_ranks(n, argv):
+    """Run this command as n ranks under torch.distributed.run (one process
+    per GPU, rendezvous on 127.0.0.1) and return its exit status: used when
+    ``--gpus n`` is given and no launcher set WORLD_SIZE."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           "--nproc-per-node", str(n), "--master-addr", "127.0.0.1",
+           "--master-port", str(free_port()),
+           os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
 
 
 def dist_setup(args):
@@ -1074,8 +1094,15 @@ def main():
     if args.nmesh is None:
         args.nmesh = 512 if args.workload == "batch" else 64
     if args.warmup < 3:
-        args.warmup = 3
+        ap.error("--warmup must be at least 3 (untimed warm-up steps)")
+    if args.gpus < 1:
+        ap.error("--gpus must be at least 1")
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
     world, rank, local, dist = dist_setup(args)
+    if world != args.gpus:
+        ap.error("--gpus %d but the launcher started %d ranks" %
+                 (args.gpus, world))
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         return

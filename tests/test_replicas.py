@@ -78,3 +78,32 @@ def test_torchrun_reference_arm_two_ranks():
     assert line["metric"] == "point-steps/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_gpus_flag_launches_its_own_ranks():
+    """``bench.py --gpus 2`` without a launcher starts its two ranks itself
+    and prints one line for both."""
+    pytest.importorskip("torch")
+    env = dict(os.environ)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR",
+              "MASTER_PORT"):
+        env.pop(k, None)
+    cmd = [sys.executable, "bench.py", "--impl", "reference", "--workload",
+           "tube1d", "--gpus", "2", "--cpu-nside", "1001", "--steps", "3",
+           "--warmup", "3"]
+    run = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True,
+                         timeout=600, env=env)
+    assert run.returncode == 0, run.stderr[-2000:]
+    lines = [json.loads(x) for x in run.stdout.splitlines()
+             if x.startswith("{")]
+    assert len(lines) == 1
+    assert lines[0]["n_gpus"] == 2 and lines[0]["impl"] == "reference"
+
+
+def test_warmup_below_three_is_rejected():
+    run = subprocess.run([sys.executable, "bench.py", "--impl", "reference",
+                          "--workload", "tube1d", "--warmup", "2",
+                          "--steps", "3"], cwd=ROOT, capture_output=True,
+                         text=True, timeout=120)
+    assert run.returncode != 0
+    assert "--warmup must be at least 3" in run.stderr
