@@ -40,6 +40,10 @@ typedef struct scg_st scg_st;
 const char * scg_last_error(void);
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t scg_launch_count(void);
+/* Number of device allocations (cudaMalloc) this library has made in this
+ * process for its solver objects and per-call scratch (the device mesh
+ * builder's Thrust buffers are not counted). */
+int64_t scg_device_alloc_count(void);
 /* Library version string. */
 const char * scg_version(void);
 
@@ -210,7 +214,9 @@ int scg_euler_sync(scg_euler * core);
  * host must be a 16-byte aligned range of one scg_host_alloc block; NULL
  * stops the delivery.  A block freed while registered is dropped at the next
  * march and never written; free a block only after scg_euler_sync, since an
- * asynchronous march may still be writing it.  The replacement for the reference's pattern of
+ * asynchronous march may still be writing it.  Batched marches
+ * (scg_batch_march) do not deliver: they refuse a core with a registered
+ * block (SCG_EINVAL) rather than leave it stale.  The replacement for the reference's pattern of
  * march(steps) followed by reading so0n / so1n (euler_march.cpp:350-359;
  * the so0n / so1n properties, multidim/pymod/wrap_multidim.cpp:393-396)
  * when the host reads every step. */
@@ -234,8 +240,10 @@ int scg_euler_totals(scg_euler * core, double * out);
  * 131,136-byte device array (held by every GPU that loads the library until
  * exit) shared by all calls: at most 67,108,864 body cells (larger meshes
  * are rejected with SCG_EINVAL), the first call on a device looks up the
- * array's address (make it before any stream capture), and calls that
- * overlap on the GPU race -- issue them one after the other. */
+ * array's address, and calls that overlap on the GPU race -- issue them one
+ * after the other.  Every call is synchronous: it copies the totals to the
+ * host and waits for the core's stream, so it must not be made while that
+ * stream is being captured into a CUDA graph. */
 int scg_euler_totals_noalloc(scg_euler * core, double * out);
 /* min and max of cflo over body cells (EulerField.calc_cfl_range). */
 int scg_euler_cfl_range(scg_euler * core, double * out);
@@ -336,7 +344,9 @@ int scg_batch_destroy(scg_batch * batch);
 int scg_batch_retarget(scg_batch * batch, scg_euler * const * cores, int64_t ncore, int * done);
 /* out[5] = ncore, total body cells, tiles, grid, block. */
 int scg_batch_info(const scg_batch * batch, int64_t * out);
-/* march(steps) of every core; synchronous. */
+/* march(steps) of every core; synchronous.  SCG_EINVAL, and nothing
+ * marched, when a core has host blocks registered with scg_euler_deliver
+ * (a batched march does not write them). */
 int scg_batch_march(scg_batch * batch, int64_t steps);
 /* Device time of the last scg_batch_march's kernels (CUDA events, ms). */
 int scg_batch_last_ms(const scg_batch * batch, double * ms);

@@ -26,6 +26,7 @@ _vp = ctypes.c_void_p
 _SIGS = {
     "scg_last_error": ([], ctypes.c_char_p),
     "scg_launch_count": ([], ctypes.c_int64),
+    "scg_device_alloc_count": ([], ctypes.c_int64),
     "scg_version": ([], ctypes.c_char_p),
     "scg_mesh_create": ([ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                          ctypes.c_int64, _vp], ctypes.c_int),
@@ -132,3 +133,8 @@ def i64buf(n):
 def launch_count():
     """Kernels launched by libscg.so so far in this process."""
     return int(lib.scg_launch_count())
+
+
+def device_alloc_count():
+    """Device allocations the library has made so far in this process."""
+    return int(lib.scg_device_alloc_count())

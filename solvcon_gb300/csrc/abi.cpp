@@ -17,6 +17,7 @@ namespace scg
 {
 
 std::atomic<int64_t> g_launches{0};
+std::atomic<int64_t> g_device_allocs{0};
 
 namespace
 {
@@ -52,6 +53,7 @@ extern "C"
 const char * scg_last_error(void) { return scg::last_error().c_str(); }
 
 int64_t scg_launch_count(void) { return scg::g_launches.load(); }
+int64_t scg_device_alloc_count(void) { return scg::g_device_allocs.load(); }
 
 const char * scg_version(void) { return "solvcon-gb300 0.1"; }
 

@@ -283,6 +283,18 @@ public:
         {
             h[p].resize(static_cast<size_t>(ncore));
         }
+        // A batched march never writes a core's registered host blocks (the
+        // step graph is shared by all cores); refuse such a core instead of
+        // leaving its blocks silently stale.
+        for (int64_t c = 0; c < ncore; ++c)
+        {
+            if (cores[static_cast<size_t>(c)]->delivering())
+            {
+                throw std::invalid_argument("EulerBatch: core " + std::to_string(c) +
+                                            " has host blocks registered with scg_euler_deliver, which batched "
+                                            "marches do not write; unregister them first");
+            }
+        }
         for (int64_t c = 0; c < ncore; ++c)
         {
             auto * core = cores[static_cast<size_t>(c)];

@@ -37,6 +37,9 @@ std::string const & last_error();
 
 // Count of kernels this library has launched (for the bench's gpu_launches).
 extern std::atomic<int64_t> g_launches;
+// Count of device allocations made through DevBuf (every device buffer of the
+// cores, batches, 1D and spacetime solvers, and per-call scratch).
+extern std::atomic<int64_t> g_device_allocs;
 
 // The device address of the host range [p, p + nbytes) when the whole range
 // lies inside one block from scg_host_alloc (page-locked and mapped into the
@@ -136,6 +139,7 @@ struct DevBuf
             (void)cudaGetLastError();
             throw std::bad_alloc();
         }
+        g_device_allocs.fetch_add(1, std::memory_order_relaxed);
         n = count;
     }
     void release()

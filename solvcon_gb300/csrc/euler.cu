@@ -1401,6 +1401,8 @@ public:
         async_pending = steps > 0 && nrow > 0;
     }
 
+    bool delivering() override { return revalidate_delivery(); }
+
     void deliver(int which, double * host, int64_t count) override
     {
         if (which != EA_SO0N && which != EA_SO1N)

@@ -120,6 +120,8 @@ public:
     // substep kernel itself, or by a gather queued after an FP32 march;
     // host = nullptr stops it.
     virtual void deliver(int which, double * host, int64_t count) = 0;
+    // True while a delivery registered with deliver() is still valid.
+    virtual bool delivering() = 0;
     virtual void sync() = 0;
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void limiter_mask(uint8_t * out) = 0;

@@ -18,8 +18,9 @@
  * TOTALS_MAX_BLOCKS * TOTALS_CHUNK = 67,108,864 body cells and rejects larger
  * meshes.  Host code cannot use the array's name as a device address; the
  * address is looked up with cudaGetSymbolAddress once per device, on the
- * first call made with that device current, so make that first call before
- * any stream capture.
+ * first call made with that device current.  Every call copies its result
+ * to the host and waits for the core's stream, so no call may be made while
+ * that stream is being captured.
  *
  * Every call on a device shares the one array and leaves its contents behind
  * for the next call.  Each call rewrites every partial row it later reads, so
@@ -42,7 +43,7 @@ namespace
 constexpr int TOTALS_THREADS = 256;
 constexpr int64_t TOTALS_CHUNK = 32768;     // body cells summed by one block
 constexpr int TOTALS_MAX_BLOCKS = 2048;     // partial-sum rows in the scratch
-constexpr int TOTALS_ROW = 8;               // doubles per row (neq <= 5, min, max)
+constexpr int TOTALS_ROW = 8;               // doubles per row: neq <= 5 used, the rest padding
 constexpr int MAX_DEVICES = 64;
 
 // Shared by every call on a device; holds the last call's contents.

@@ -249,3 +249,31 @@ def test_deliver_rejects_bad_targets():
                                         n0))
     finally:
         blk.free()
+
+
+def test_batched_march_refuses_a_delivering_core():
+    """A batched march does not write registered host blocks: it refuses a
+    core that has one (ValueError, nothing marched), and marches it once
+    the block is unregistered."""
+    from solvcon_gb300._lib import check, lib
+    from solvcon_gb300.batch import EulerBatch
+    a = _marched_core("fp32", 2)
+    b = _marched_core("fp32", 2)
+    batch = EulerBatch([a, b], block=64, persistent=True)
+    shape = _shape(b, "so0n")
+    blk = _Block(int(np.prod(shape)))
+    try:
+        before = _get(b, RECORD_TABLES["so0n"], shape)
+        check(lib.scg_euler_deliver(b.handle, RECORD_TABLES["so0n"],
+                                    ctypes.c_void_p(blk.addr),
+                                    blk.view.size))
+        with pytest.raises(ValueError, match="scg_euler_deliver"):
+            batch.march(1)
+        np.testing.assert_array_equal(
+            _get(b, RECORD_TABLES["so0n"], shape), before)
+        check(lib.scg_euler_deliver(b.handle, RECORD_TABLES["so0n"], None, 0))
+        batch.march(1)
+        assert not np.array_equal(_get(b, RECORD_TABLES["so0n"], shape),
+                                  before)
+    finally:
+        blk.free()

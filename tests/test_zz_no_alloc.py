@@ -53,13 +53,19 @@ def _core(ndim, nside, precision):
 
 def _check_pair(lib, core):
     ref = np.zeros(core.neq)
+    a0 = lib.device_alloc_count()
     lib.check(lib.lib.scg_euler_totals(core.handle, lib.ptr(ref)))
+    # The allocating entry point is seen by the counter.
+    assert lib.device_alloc_count() > a0
     mags = np.abs(np.array(core.so0n.ndarray)[core.ngstcell:]).sum(axis=0)
     for _ in range(2):  # two calls in a row
         got = np.full(core.neq, np.nan)
         n0 = lib.launch_count()
+        a0 = lib.device_alloc_count()
         lib.check(lib.lib.scg_euler_totals_noalloc(core.handle, lib.ptr(got)))
         assert lib.launch_count() - n0 == 2
+        # The point of the entry point: no device allocation at all.
+        assert lib.device_alloc_count() == a0
         # The tolerance of the march parity tests: relative 1e-12, with an
         # absolute floor for totals that cancel (momentum at rest).
         np.testing.assert_allclose(got, ref, rtol=1e-12,
