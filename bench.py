@@ -47,10 +47,13 @@ sys.path.insert(0, ROOT)
 # Algorithmic HBM bytes of one cell-substep of the fused march: compulsory
 # reads of the neighbour-summed state, the cell's geometry and ids, and writes
 # of so0n, so1n, cflo, cflc.  2D triangles: FP64 520 B, FP32 state with FP64
-# geometry 412 B, all FP32 268 B; 3D tetrahedra: 1,100 / 928 / 560 B.
-ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
-             ("tri2d", "fp32"): 268, ("tet3d", "fp64"): 1100,
-             ("tet3d", "fp32-geom64"): 928, ("tet3d", "fp32"): 560}
+# geometry (the FP32 form, "fp32") 412 B, FP32 geometry too ("fp32-geom32")
+# 268 B; 3D tetrahedra: 1,100 / 928 / 560 B.
+ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32"): 412,
+             ("tri2d", "fp32-geom32"): 268, ("tet3d", "fp64"): 1100,
+             ("tet3d", "fp32"): 928, ("tet3d", "fp32-geom32"): 560}
+ALG_BYTES.update({(w, "fp32-geom64"): ALG_BYTES[(w, "fp32")]
+                  for w in ("tri2d", "tet3d")})
 
 # DRAM bytes (read + write) and FP64 flops (DFMA counted as 2) of the fused
 # substep kernel per cell-substep, each from one ncu capture of the kernel on
@@ -59,8 +62,10 @@ ALG_BYTES = {("tri2d", "fp64"): 520, ("tri2d", "fp32-geom64"): 412,
 # cells; absent until captured.  The FP64 records carry a primitive cache
 # (192 B instead of 128 B), which trades DRAM bytes, idle in the FP64-bound
 # march, for FP64 operations.
-NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 769.5, ("tri2d", "fp32"): 270.2,
-                        ("tet3d", "fp64"): 1337.3, ("tet3d", "fp32"): 627.1}
+NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 769.5,
+                        ("tri2d", "fp32-geom32"): 270.2,
+                        ("tet3d", "fp64"): 1337.3,
+                        ("tet3d", "fp32-geom32"): 627.1}
 NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1159.6, ("tet3d", "fp64"): 2717.4}
 
 WORKLOADS = {
@@ -859,45 +864,138 @@ def _body(core):
     return np.array(core.so0n[...])[core.ngstcell:]
 
 
+FP32_FORMS = ("fp32", "fp32-geom32")
+
+# Gradient magnitude, relative to the equation's largest, above which a
+# (cell, equation) pair's W-3/4 firing decision is not round-off: in a cell
+# whose state is still uniform the per-element gradients are noise, their
+# inverse-magnitude weights scatter by O(1) and the cap binds at random (the
+# reference itself flips those bits under a 1e-15 input perturbation).
+RESOLVED_GRADIENT = 1e-10
+
+
+def _totals_rel(got, ref_q):
+    """Relative difference of totals against sum(ref_q) per variable; a
+    total that cancels is measured against the magnitudes it sums."""
+    tref = ref_q.sum(0)
+    scale = np.maximum(np.abs(tref), np.abs(ref_q).sum(0))
+    return [float(x) for x in np.abs(np.asarray(got) - tref) / scale]
+
+
+def _limiter_hamming(mask, ref_mask, ref_so1n, neq):
+    """Hamming fraction of two W-3/4 firing masks over (cell, equation)
+    pairs: over all pairs, and over the pairs whose gradient is resolved."""
+    bits = lambda m: np.unpackbits(  # noqa: E731
+        np.asarray(m, dtype=np.uint8)[:, None], axis=1,
+        bitorder="little")[:, :neq].astype(bool)
+    diff = bits(mask) != bits(ref_mask)
+    grad = np.linalg.norm(ref_so1n, axis=2)
+    res = grad > RESOLVED_GRADIENT * grad.max(axis=0)[None, :]
+    return {"all": float(diff.mean()),
+            "resolved": float(diff[res].mean()) if res.any() else 0.0,
+            "resolved_fraction": float(res.mean()),
+            "fired_fraction": float(bits(ref_mask).mean())}
+
+
 def run_accuracy(args, world, rank, dist):
-    """Accuracy of the FP32-state march against FP64, beside the problem's
-    own sensitivity (the FP64 march from an initial state perturbed by 1e-15
-    relative), on three cases:
+    """Accuracy of the GPU marches, beside the problem's own sensitivity (the
+    FP64 march from an initial state perturbed by 1e-15 relative):
 
-    * the 3D spherical blast at full size (160^3 x 6 tetrahedra, CFL 0.7,
-      200 steps): relative L1/Linf per variable, FP64 totals of each march;
-    * the batched distribution (64 meshes, CFL 0.8, 1000 steps): aggregate
-      and worst-mesh relative L1 per variable; meshes on which the FP64 march
-      itself becomes non-finite (the fixed dt outgrows the CFL limit as the
-      flow evolves; the CPU oracle fails on the same meshes at the same steps)
-      are listed and left out;
-    * a sample of the 2D four-quadrant workload (300 x 300 x 2 triangles,
-      CFL 0.8, 500 steps) against the CPU oracle itself.
+    * ``oracle2d``: a sample of the 2D four-quadrant workload (300 x 300 x 2
+      triangles, CFL 0.8, 500 steps) against the CPU oracle itself;
+    * ``oracle3d``: the 3D spherical blast at 40^3 x 6 = 384,000 tetrahedra
+      (CFL 0.7, 200 steps) against the CPU oracle itself;
+      both report per conserved variable the relative L1/Linf, the totals
+      sum(so0n * clvol) against the oracle's, and the W-3/4 firing pattern's
+      Hamming fraction (all pairs, and resolved pairs), for FP64, FP64 from
+      the perturbed state, and both FP32 forms;
+    * ``blast3d``: the 3D blast at full size (160^3 x 6 tetrahedra, 200
+      steps): both FP32 forms and perturbed FP64 against FP64, with the
+      totals' difference every 20 steps;
+    * ``batch``: the batched distribution (64 meshes, CFL 0.8, 1000 steps):
+      aggregate and worst-mesh relative L1 per variable of the FP32 forms
+      (batched) and of perturbed FP64 against FP64; meshes on which the FP64
+      march itself becomes non-finite (the fixed dt outgrows the CFL limit;
+      the oracle fails on the same meshes at the same steps) are left out.
 
-    The FP64 GPU march is the reference at full size (the CPU oracle would
-    take hours); parity tests pin it to the oracle on smaller meshes.
-    ``--cases`` picks a subset (blast3d, batch, oracle2d; default all)."""
+    At full size the FP64 GPU march stands in for the oracle (the oracle
+    would take hours); the oracle cases and the parity tests pin it.  The
+    oracle runs on every host core (its per-cell loops are threaded; the
+    results do not depend on the thread count).  ``--cases`` picks a subset
+    (default all)."""
     from oracle import oracle as ora
     if rank != 0:
         return
+    ora.set_threads(len(os.sched_getaffinity(0)))
     out = {"metric": "accuracy", "data": "synthetic"}
     rng = np.random.default_rng(1)
-    cases = set((args.cases or "blast3d,batch,oracle2d").split(","))
-    unknown = cases - {"blast3d", "batch", "oracle2d"}
+    allc = ("oracle2d", "oracle3d", "blast3d", "batch")
+    cases = set((args.cases or ",".join(allc)).split(","))
+    unknown = cases - set(allc)
     if unknown:
         raise SystemExit("--cases: unknown %s" % sorted(unknown))
-    if "blast3d" in cases:
-        _accuracy_blast3d(args, out, rng)
-    if "batch" in cases:
-        _accuracy_batch(args, out, rng)
-    if "oracle2d" in cases:
-        _accuracy_oracle2d(args, out, rng, ora)
+    for c in allc:
+        if c in cases:
+            t0 = time.perf_counter()
+            {"oracle2d": _accuracy_oracle2d, "oracle3d": _accuracy_oracle3d,
+             "blast3d": _accuracy_blast3d, "batch": _accuracy_batch}[c](
+                 args, out, rng, ora)
+            out[c]["seconds"] = time.perf_counter() - t0
+            print(json.dumps({c: out[c]}), file=sys.stderr, flush=True)
     print(json.dumps(out), flush=True)
 
 
-def _accuracy_blast3d(args, out, rng):
-    """The 3D spherical blast at full size: FP32 and perturbed FP64 against
-    FP64."""
+def _against_oracle(workload, nside, steps, rng, ora):
+    w, mesh, state, faces = make_workload(workload, nside=nside)
+    nd, ng = mesh.ndim, mesh.ngstcell
+    dt = dt_for_cfl(mesh, state, faces, w["cfl"])
+    vol = np.array(mesh.clvol.ndarray)[ng:]
+    o = ora.OracleEuler(mesh, dt)
+    o.init_solution(1.4, 1.0, [0.0] * nd, 1.0)
+    o.so0n[ng:] = state
+    o.add_slipwall(faces)
+    o.call("bc_soln")
+    o.call("bc_dsoln")
+    t0 = time.perf_counter()
+    o.march(steps)
+    oracle_s = time.perf_counter() - t0
+    want = np.array(o.so0n)[ng:]
+    so1n = np.array(o.so1n)[ng:]
+    q = want * vol[:, None]
+    res = {"cells": mesh.ncell, "steps": steps, "cfl": w["cfl"],
+           "oracle_s": oracle_s,
+           "oracle_totals_change": _totals_rel(q.sum(0),
+                                               state * vol[:, None])}
+    pert = state * (1 + 1e-15 * rng.uniform(-1, 1, state.shape))
+    for name, prec, st in (("gpu_fp64", "fp64", state),
+                           ("gpu_fp64_perturbed", "fp64", pert)) + tuple(
+                               ("gpu_" + f.replace("-", "_"), f, state)
+                               for f in FP32_FORMS):
+        c = setup_core(mesh, st, faces, dt, prec)
+        c.march(steps)
+        l1, linf = _rel_l1_linf(_body(c), want, vol)
+        res[name + "_vs_oracle"] = {
+            "rel_l1": l1, "rel_linf": linf,
+            "totals_rel": _totals_rel(c.totals(), q),
+            "limiter_hamming": _limiter_hamming(c.limiter_mask(), o.limiter[
+                :mesh.ncell], so1n, nd + 2)}
+        del c
+    return res
+
+
+def _accuracy_oracle2d(args, out, rng, ora):
+    """A sample of the 2D four-quadrant workload against the CPU oracle."""
+    out["oracle2d"] = _against_oracle("tri2d", 300, 500, rng, ora)
+
+
+def _accuracy_oracle3d(args, out, rng, ora):
+    """The 3D blast at 40^3 x 6 tetrahedra against the CPU oracle."""
+    out["oracle3d"] = _against_oracle("tet3d", 40, 200, rng, ora)
+
+
+def _accuracy_blast3d(args, out, rng, ora=None):
+    """The 3D spherical blast at full size: the FP32 forms and perturbed
+    FP64 against FP64, totals every 20 steps."""
     nside = args.nside or 160
     t0 = time.perf_counter()
     w, mesh, state, faces = make_workload("tet3d", nside=nside)
@@ -907,43 +1005,50 @@ def _accuracy_blast3d(args, out, rng):
     pert = state * (1 + 1e-15 * rng.uniform(-1, 1, state.shape))
     res = {"cells": mesh.ncell, "steps": 200, "cfl": 0.7, "build_s": build_s}
     finals, tots = {}, {}
-    for name, prec, st in (("fp64", "fp64", state), ("fp64_perturbed", "fp64",
-                                                      pert),
-                           ("fp32", "fp32", state)):
+    for name, prec, st in (("fp64", "fp64", state),
+                           ("fp64_perturbed", "fp64", pert)) + tuple(
+                               (f.replace("-", "_"), f, state)
+                               for f in FP32_FORMS):
         c = setup_core(mesh, st, faces, dt, prec)
-        tot0 = np.array(c.totals())
-        c.march(200)
-        tots[name] = np.array(c.totals())
-        res[name + "_mass_energy_change"] = [
-            float(x) for x in ((tots[name] - tot0) / np.abs(tot0))[[0, 4]]]
+        series = [np.array(c.totals())]
+        for _ in range(10):
+            c.march(20)
+            series.append(np.array(c.totals()))
+        tots[name] = np.array(series)
         finals[name] = _body(c)
         del c
-    for name in ("fp64_perturbed", "fp32"):
+    t64 = tots["fp64"]
+    res["fp64_mass_energy_change"] = [
+        float(x) for x in ((t64[-1] - t64[0]) / np.abs(t64[0]))[[0, 4]]]
+    for name in finals:
+        if name == "fp64":
+            continue
         l1, linf = _rel_l1_linf(finals[name], finals["fp64"], vol)
-        res[name + "_vs_fp64"] = {"rel_l1": l1, "rel_linf": linf}
-        res[name + "_totals_vs_fp64"] = [
-            float(x) for x in ((tots[name] - tots["fp64"]) /
-                               np.abs(tots["fp64"]))[[0, 4]]]
+        res[name + "_vs_fp64"] = {
+            "rel_l1": l1, "rel_linf": linf,
+            "mass_energy_totals_every_20_steps": [
+                [float(x) for x in col] for col in
+                ((tots[name] - t64) / np.abs(t64))[:, [0, 4]].T]}
     out["blast3d"] = res
     del finals
 
 
-def _accuracy_batch(args, out, rng):
-    """The batched distribution, 1000 steps: FP32 (batched) and perturbed
-    FP64 against FP64."""
+def _accuracy_batch(args, out, rng, ora=None):
+    """The batched distribution, 1000 steps: the FP32 forms (batched) and
+    perturbed FP64 against FP64."""
     from solvcon_gb300.batch import EulerBatch
     nmesh = args.nmesh
     data = batch_meshes(nmesh)
     dts = [dt_for_cfl_g(m, s, 0.8, g) for m, s, f, g in data]
     finals = {}
-    for name, prec in (("fp64", "fp64"), ("fp64_perturbed", "fp64"),
-                       ("fp32", "fp32")):
+    for name, prec in (("fp64", "fp64"), ("fp64_perturbed", "fp64")) + tuple(
+            (f.replace("-", "_"), f) for f in FP32_FORMS):
         cs = []
         for (m, s, f, g), dtk in zip(data, dts):
             st = s * (1 + 1e-15 * rng.uniform(-1, 1, s.shape)) \
                 if name == "fp64_perturbed" else s
             cs.append(setup_core_g(m, st, f, dtk, prec, g))
-        if prec == "fp32":
+        if prec != "fp64":
             EulerBatch(cs, block=64, persistent=True).march(1000)
         else:
             for c in cs:
@@ -952,10 +1057,12 @@ def _accuracy_batch(args, out, rng):
         del cs
     ok = [k for k in range(nmesh) if np.isfinite(finals["fp64"][k]).all()]
     res = {"meshes": nmesh, "steps": 1000, "cfl": 0.8,
-           "fp64_nonfinite_meshes": [k for k in range(nmesh) if k not in ok],
-           "fp32_nonfinite_meshes": [k for k in range(nmesh) if not
-                                     np.isfinite(finals["fp32"][k]).all()]}
-    for name in ("fp64_perturbed", "fp32"):
+           "fp64_nonfinite_meshes": [k for k in range(nmesh) if k not in ok]}
+    for name in finals:
+        if name == "fp64":
+            continue
+        res[name + "_nonfinite_meshes"] = [
+            k for k in range(nmesh) if not np.isfinite(finals[name][k]).all()]
         num = np.zeros(4)
         den = np.zeros(4)
         worst = np.zeros(4)
@@ -974,37 +1081,6 @@ def _accuracy_batch(args, out, rng):
     out["batch"] = res
     del finals
 
-
-def _accuracy_oracle2d(args, out, rng, ora):
-    """A sample of the 2D four-quadrant workload against the CPU oracle."""
-    steps = 500
-    w, mesh, state, faces = make_workload("tri2d", nside=300)
-    dt = dt_for_cfl(mesh, state, faces, 0.8)
-    vol = np.array(mesh.clvol.ndarray)[mesh.ngstcell:]
-    ng = mesh.ngstcell
-    o = ora.OracleEuler(mesh, dt)
-    o.init_solution(1.4, 1.0, [0.0, 0.0], 1.0)
-    o.so0n[ng:] = state
-    o.add_slipwall(faces)
-    o.call("bc_soln")
-    o.call("bc_dsoln")
-    t0 = time.perf_counter()
-    o.march(steps)
-    oracle_s = time.perf_counter() - t0
-    want = np.array(o.so0n)[ng:]
-    res = {"cells": mesh.ncell, "steps": steps, "cfl": 0.8,
-           "oracle_s": oracle_s}
-    for name, prec, st in (("gpu_fp64", "fp64", state),
-                           ("gpu_fp64_perturbed", "fp64",
-                            state * (1 + 1e-15 * rng.uniform(-1, 1,
-                                                             state.shape))),
-                           ("gpu_fp32", "fp32", state)):
-        c = setup_core(mesh, st, faces, dt, prec)
-        c.march(steps)
-        l1, linf = _rel_l1_linf(_body(c), want, vol)
-        res[name + "_vs_oracle"] = {"rel_l1": l1, "rel_linf": linf}
-        del c
-    out["quadrant2d_vs_oracle"] = res
 
 def run_meshbuild(args, world, rank, dist):
     """Time to first step of the 3D workload's mesh (160^3 x 6 tetrahedra by
@@ -1076,7 +1152,10 @@ def main():
                                                  "accuracy", "meshbuild"] +
                     sorted(LINE_WORKLOADS))
     ap.add_argument("--precision", default=None,
-                    choices=["fp64", "fp32", "fp32-geom64"])
+                    choices=["fp64", "fp32", "fp32-geom64", "fp32-geom32"],
+                    help="fp32: FP32 state and flux with FP64 geometry "
+                    "tables (fp32-geom64 is the same); fp32-geom32 also "
+                    "stores the geometry in FP32")
     ap.add_argument("--nside", type=int, default=None)
     ap.add_argument("--cpu-nside", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=20)
@@ -1084,7 +1163,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cases", default=None,
                     help="accuracy workload: comma-separated subset of "
-                    "blast3d, batch, oracle2d")
+                    "oracle2d, oracle3d, blast3d, batch")
     ap.add_argument("--nmesh", type=int, default=None)
     ap.add_argument("--nreq", type=int, default=64)
     ap.add_argument("--rates", default="50,200,1000,2000")

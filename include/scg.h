@@ -73,6 +73,22 @@ const char * scg_version(void);
 /* StaticMesh(ndim, nnode, nface, ncell): StaticMesh.hpp:290-311. */
 int scg_mesh_create(int ndim, int64_t nnode, int64_t nface, int64_t ncell, scg_mesh ** out);
 int scg_mesh_destroy(scg_mesh * mesh);
+/* A mesh built by other code -- the reference's own StaticMesh after
+ * build_interior, build_boundary and build_ghost (its Gmsh reader's, a
+ * pilot driver's), or anything producing the same tables -- taken over
+ * verbatim, nothing rebuilt.  sizes[9] = ndim nnode nface ncell nbound
+ * ngstnode ngstface ngstcell nedge (the size properties,
+ * wrap_StaticMesh.cpp:97-106); tables[15] = the whole buffers, ghost rows
+ * first, in SCG_MESH_* order, in the layout of the reference's table
+ * properties (StaticMesh.hpp:434-451; float64 for ndcrd..clvol, int32 for
+ * fctpn..bndfcs); a table with no rows may be null.  The tables are copied;
+ * the core built on the mesh checks the connectivity on the device before
+ * any kernel indexes through it. */
+int scg_mesh_from_tables(const int64_t * sizes, const void * const * tables, scg_mesh ** out);
+/* Append a boundary group with its facn table [nbound][3] verbatim (the
+ * reference's StaticMeshBC name and facn, StaticMesh.hpp:159-251), for a mesh
+ * taken over with scg_mesh_from_tables. */
+int scg_mesh_adopt_bc(scg_mesh * mesh, const char * name, const int32_t * facn, int64_t nbound);
 /* out[10] = ndim nnode nface ncell nbound ngstnode ngstface ngstcell nedge nbcs
  * (wrap_StaticMesh.cpp:97-106). */
 int scg_mesh_sizes(const scg_mesh * mesh, int64_t * out);
@@ -127,8 +143,16 @@ int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
 
 /* Precision of the march. */
 #define SCG_FP64 0        /* the reference's FP64 arithmetic */
-#define SCG_FP32_GEOM64 1 /* FP32 state and flux, FP64 geometry tables */
-#define SCG_FP32 2        /* FP32 state, flux and stored geometry (computed FP64) */
+/* The FP32 form of the EulerCore: FP32 state and flux arithmetic with
+ * compensated face sums, mesh geometry kept in FP64 tables, FP64 totals and
+ * CFL reduction. */
+#define SCG_FP32_GEOM64 1
+/* A faster EulerCore variant beside it: the same FP32 march with its
+ * geometry (computed in FP64) stored in FP32, ~35% less traffic per cell. */
+#define SCG_FP32_GEOM32 2
+/* Euler1DCore's FP32 state (its coordinates stay FP64), and the FP32 pipe of
+ * scg_fma_peak; as an EulerCore precision the same code as SCG_FP32_GEOM32. */
+#define SCG_FP32 2
 
 /* EulerCore array ids (wrap_multidim.cpp:381-408). */
 #define SCG_EA_CEVOL 0

@@ -15,6 +15,15 @@
 #define CLMFC 6
 #define FCMND 4
 
+/* Threads the per-cell loops of the multidim march may use (1 by default,
+ * the reference's serial loop).  Every cell's arithmetic is the same either
+ * way -- each loop iteration writes only its own cell's rows -- so the
+ * results are bit-identical for any count; the checker uses more threads only
+ * to reach larger meshes in reasonable time. */
+static int g_threads = 1;
+
+void ora_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+
 /* ---- mesh accessors (ghost rows first) --------------------------------- */
 
 static inline double ndcrd(const ora_mesh * m, int64_t i, int d) { return m->ndcrd[(i + m->ngstnode) * m->ndim + d]; }
@@ -266,9 +275,10 @@ static void jaco_update(jaco_t * J, int nd, double gamma, const double * sol)
 void ora_calc_solt(ora_euler * e)
 {
     int const nd = NDIMX(e), neq = NEQX(e);
-    jaco_t J;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int64_t icl = -e->m.ngstcell; icl < e->m.ncell; ++icl)
     {
+        jaco_t J;
         double sol[5];
         for (int k = 0; k < neq; ++k)
             sol[k] = SO0(e->so0c, e, icl, k);
@@ -292,9 +302,10 @@ void ora_calc_soln(ora_euler * e)
     double const dt = e->dt;
     double const qdt = dt * 0.25;
     double const hdt = dt * 0.5;
-    jaco_t J;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int64_t icl = 0; icl < m->ncell; ++icl)
     {
+        jaco_t J;
         int32_t const clnfc = clfcs(m, icl, 0);
         double acc[5] = {0, 0, 0, 0, 0};
         for (int ifl = 1; ifl <= clnfc; ++ifl)
@@ -538,6 +549,7 @@ void ora_calc_cfl(ora_euler * e)
     int const nd = NDIMX(e), neq = NEQX(e);
     double const TINY = 1.e-60;
     double const hdt = e->dt / 2.0;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int64_t icl = 0; icl < m->ncell; ++icl)
     {
         int32_t const clnfc = clfcs(m, icl, 0);
@@ -741,6 +753,7 @@ void ora_calc_dsoln(ora_euler * e)
     int const nd = NDIMX(e), neq = NEQX(e);
     double const ALMOST_ZERO = 1.e-200;
     double const hdt = e->dt * 0.5;
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1)
     for (int64_t icl = 0; icl < m->ncell; ++icl)
     {
         double const acfl = fabs(e->cflc[ROW(e, icl)]);

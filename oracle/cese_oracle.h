@@ -68,6 +68,9 @@ void ora_bc_dsoln(ora_euler * e);
 void ora_update(ora_euler * e);
 void ora_march_substep(ora_euler * e);
 void ora_march(ora_euler * e, int64_t steps);
+/* Threads for the per-cell loops of the multidim march (default 1); the
+ * results do not depend on it. */
+void ora_set_threads(int n);
 
 /* 1D Euler core (onedim/Euler1DCore.*). */
 typedef struct

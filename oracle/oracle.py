@@ -40,6 +40,8 @@ def lib():
             getattr(_lib, name).restype = None
         _lib.ora_march.argtypes = [ctypes.c_void_p, ctypes.c_int64]
         _lib.ora_march.restype = None
+        _lib.ora_set_threads.argtypes = [ctypes.c_int]
+        _lib.ora_set_threads.restype = None
         _lib.ora_e1d_march.argtypes = [ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_int64]
         _lib.ora_e1d_update_cfl.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -50,6 +52,13 @@ def lib():
         _lib.ora_e1d_treat_boundary_so0.argtypes = [ctypes.c_void_p]
         _lib.ora_e1d_treat_boundary_so1.argtypes = [ctypes.c_void_p]
     return _lib
+
+
+def set_threads(n):
+    """Threads for the per-cell loops of the multidim march (1 by default,
+    the reference's serial order per cell; the results are bit-identical for
+    any count)."""
+    lib().ora_set_threads(int(n))
 
 
 _P = ctypes.c_void_p

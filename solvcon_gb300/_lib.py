@@ -31,6 +31,9 @@ _SIGS = {
     "scg_mesh_create": ([ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                          ctypes.c_int64, _vp], ctypes.c_int),
     "scg_mesh_destroy": ([_vp], ctypes.c_int),
+    "scg_mesh_from_tables": ([_vp, _vp, _vp], ctypes.c_int),
+    "scg_mesh_adopt_bc": ([_vp, ctypes.c_char_p, _vp, ctypes.c_int64],
+                          ctypes.c_int),
     "scg_mesh_sizes": ([_vp, _vp], ctypes.c_int),
     "scg_mesh_array": ([_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
                        ctypes.c_int),

@@ -65,6 +65,80 @@ int scg_mesh_create(int ndim, int64_t nnode, int64_t nface, int64_t ncell, scg_m
     });
 }
 
+int scg_mesh_from_tables(const int64_t * sizes, const void * const * tables, scg_mesh ** out)
+{
+    return guarded([&] {
+        need(sizes, "scg_mesh_from_tables");
+        need(tables, "scg_mesh_from_tables");
+        need(out, "scg_mesh_from_tables");
+        int64_t const ndim = sizes[0], nnode = sizes[1], nface = sizes[2], ncell = sizes[3], nbound = sizes[4];
+        int64_t const ngnode = sizes[5], ngface = sizes[6], ngcell = sizes[7], nedge = sizes[8];
+        for (int k = 1; k < 9; ++k)
+        {
+            if (sizes[k] < 0)
+            {
+                throw std::invalid_argument("StaticMesh: negative size in scg_mesh_from_tables");
+            }
+        }
+        auto h = std::make_unique<scg_mesh>(scg_mesh{scg::HostMesh(static_cast<int>(ndim), nnode, nface, ncell)});
+        scg::HostMesh & m = h->m;
+        m.nbound = nbound;
+        m.ngstnode = ngnode;
+        m.ngstface = ngface;
+        m.ngstcell = ngcell;
+        int const nd = static_cast<int>(ndim);
+        // Shapes after build_ghost (StaticMesh.hpp:434-451): node, face and
+        // cell tables carry their ghost rows first.
+        auto take = [&](auto & t, int which, int64_t ngst, int64_t nbody, int64_t width) {
+            using T = typename std::decay_t<decltype(t.buf)>::value_type;
+            t.make_unset(ngst, nbody, width);
+            size_t const n = static_cast<size_t>((ngst + nbody) * width);
+            if (n == 0)
+            {
+                return;
+            }
+            T const * src = static_cast<T const *>(tables[which]);
+            if (!src)
+            {
+                throw std::invalid_argument("scg_mesh_from_tables: table " + std::to_string(which) + " is null");
+            }
+            std::copy(src, src + n, t.buf.begin());
+        };
+        take(m.ndcrd, SCG_MESH_NDCRD, ngnode, nnode, nd);
+        take(m.fccnd, SCG_MESH_FCCND, ngface, nface, nd);
+        take(m.fcnml, SCG_MESH_FCNML, ngface, nface, nd);
+        take(m.fcara, SCG_MESH_FCARA, ngface, nface, 1);
+        take(m.clcnd, SCG_MESH_CLCND, ngcell, ncell, nd);
+        take(m.clvol, SCG_MESH_CLVOL, ngcell, ncell, 1);
+        take(m.fctpn, SCG_MESH_FCTPN, ngface, nface, 1);
+        take(m.cltpn, SCG_MESH_CLTPN, ngcell, ncell, 1);
+        take(m.clgrp, SCG_MESH_CLGRP, ngcell, ncell, 1);
+        take(m.fcnds, SCG_MESH_FCNDS, ngface, nface, scg::FCMND + 1);
+        take(m.fccls, SCG_MESH_FCCLS, ngface, nface, scg::FCREL);
+        take(m.clnds, SCG_MESH_CLNDS, ngcell, ncell, scg::CLMND + 1);
+        take(m.clfcs, SCG_MESH_CLFCS, ngcell, ncell, scg::CLMFC + 1);
+        take(m.ednds, SCG_MESH_EDNDS, 0, nedge, 2);
+        take(m.bndfcs, SCG_MESH_BNDFCS, 0, nbound, scg::BFREL);
+        *out = h.release();
+    });
+}
+
+int scg_mesh_adopt_bc(scg_mesh * mesh, const char * name, const int32_t * facn, int64_t nbound)
+{
+    return guarded([&] {
+        auto & m = need(mesh, "scg_mesh_adopt_bc")->m;
+        need(name, "scg_mesh_adopt_bc");
+        if (nbound < 0 || (nbound > 0 && !facn))
+        {
+            throw std::invalid_argument("scg_mesh_adopt_bc: facn must hold nbound rows");
+        }
+        scg::BcGroup g;
+        g.name = name;
+        g.facn.assign(facn, facn + nbound * scg::BFREL);
+        m.bcs.push_back(std::move(g));
+    });
+}
+
 int scg_mesh_destroy(scg_mesh * mesh)
 {
     return guarded([&] { delete mesh; });

@@ -81,8 +81,8 @@ enum EulerField : int
 enum Precision : int
 {
     PREC_FP64 = 0,         // everything FP64 (the reference's arithmetic)
-    PREC_FP32_GEOM64 = 1,  // FP32 state and flux, FP64 geometry in HBM
-    PREC_FP32 = 2,         // FP32 state and flux, FP64-computed geometry stored FP32
+    PREC_FP32_GEOM64 = 1,  // FP32 state and flux, FP64 geometry in HBM (the FP32 form)
+    PREC_FP32 = 2,         // FP32 state and flux, FP64-computed geometry stored FP32 (faster variant)
 };
 
 struct EulerBoundary

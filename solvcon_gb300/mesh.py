@@ -74,6 +74,65 @@ class StaticMesh:
                                   int(ncell), ctypes.byref(h)))
         self._h = h
 
+    _SIZES = ("ndim", "nnode", "nface", "ncell", "nbound", "ngstnode",
+              "ngstface", "ngstcell", "nedge")
+
+    @classmethod
+    def from_mesh(cls, other):
+        """Not in the reference: take over a mesh built by other code -- the
+        reference's own ``solvcon.StaticMesh`` (from its Gmsh reader, a pilot
+        driver, or ``build_interior``/``build_boundary``/``build_ghost``) or
+        any object with the same surface -- with every table copied
+        verbatim and nothing rebuilt, so that its cells, faces and ghost
+        layer march on the GPU exactly as numbered there.
+
+        ``other`` needs the size properties (``ndim`` ... ``nedge``), the
+        fifteen table properties whose ``.ndarray`` is the whole buffer with
+        the ghost rows first (wrap_StaticMesh.cpp:61-181), and optionally
+        ``bcs`` (objects with ``name`` and ``facn``)."""
+        sizes = np.array([int(getattr(other, k)) for k in cls._SIZES],
+                         dtype="int64")
+        nd, nnode, nface, ncell, nbound, gnode, gface, gcell, nedge = \
+            (int(x) for x in sizes)
+        rows = {"node": gnode + nnode, "face": gface + nface,
+                "cell": gcell + ncell}
+        shape = {"ndcrd": ("node", nd), "fccnd": ("face", nd),
+                 "fcnml": ("face", nd), "fcara": ("face", 1),
+                 "clcnd": ("cell", nd), "clvol": ("cell", 1),
+                 "fctpn": ("face", 1), "cltpn": ("cell", 1),
+                 "clgrp": ("cell", 1), "fcnds": ("face", cls.FCMND + 1),
+                 "fccls": ("face", cls.FCREL),
+                 "clnds": ("cell", cls.CLMND + 1),
+                 "clfcs": ("cell", cls.CLMFC + 1)}
+        keep = []
+        ptrs = (ctypes.c_void_p * len(_ARRAYS))()
+        for i, name in enumerate(_ARRAYS):
+            dtype = "int32" if i >= _ARRAYS.index("fctpn") else "float64"
+            arr = getattr(other, name)
+            arr = getattr(arr, "ndarray", arr)
+            buf = np.ascontiguousarray(arr, dtype=dtype)
+            if name == "ednds":
+                want = nedge * 2
+            elif name == "bndfcs":
+                want = nbound * cls.BFREL
+            else:
+                kind, width = shape[name]
+                want = rows[kind] * width
+            if buf.size != want:
+                raise ValueError("StaticMesh.from_mesh: %s holds %d values, "
+                                 "the sizes need %d" % (name, buf.size, want))
+            keep.append(buf)
+            ptrs[i] = buf.ctypes.data if buf.size else None
+        h = ctypes.c_void_p()
+        check(lib.scg_mesh_from_tables(ptr(sizes), ptrs, ctypes.byref(h)))
+        self = cls._adopt(h)
+        for bc in getattr(other, "bcs", ()) or ():
+            facn = getattr(bc.facn, "ndarray", bc.facn)
+            facn = np.ascontiguousarray(facn, dtype="int32").reshape(-1, 3)
+            check(lib.scg_mesh_adopt_bc(h, str(bc.name).encode(), ptr(facn),
+                                        facn.shape[0]))
+        return self
+
     @classmethod
     def _adopt(cls, handle):
         """Wrap a native scg_mesh handle (the wrapper destroys it)."""

@@ -33,7 +33,9 @@ _ID = {n: i for i, n in enumerate(ARRAYS)}
 _OPS = {"prepare_ce": 0, "update": 1, "calc_solt": 2, "calc_soln": 3,
         "bc_soln": 4, "calc_cfl": 5, "calc_dsoln": 6, "bc_dsoln": 7,
         "march_substep": 8, "reset_state": 9}
-PRECISIONS = {"fp64": 0, "fp32-geom64": 1, "fp32": 2}
+# "fp32" is the FP32 form (FP32 state and flux, FP64 geometry tables);
+# "fp32-geom64" names the same; "fp32-geom32" also stores the geometry FP32.
+PRECISIONS = {"fp64": 0, "fp32": 1, "fp32-geom64": 1, "fp32-geom32": 2}
 _SWAP = (("so0c", "so0n"), ("so1c", "so1n"))
 
 
@@ -41,11 +43,17 @@ class EulerCore:
     """Solve the Euler equations with the CESE method on the GPU.
 
     :param mesh: a :class:`~solvcon_gb300.mesh.StaticMesh` with its ghost
-        layer built.
+        layer built, or a mesh built by other code with the reference
+        StaticMesh surface (the reference's own ``solvcon.StaticMesh``),
+        whose tables are then taken over verbatim
+        (:meth:`StaticMesh.from_mesh`).
     :param time_increment: the fixed time step.
     :param precision: ``"fp64"`` (the reference's arithmetic), ``"fp32"``
-        (FP32 state and flux, FP64-computed geometry stored in FP32) or
-        ``"fp32-geom64"`` (FP32 state and flux, FP64 geometry tables).
+        (not in the reference: FP32 state and flux arithmetic with
+        compensated face sums, the mesh geometry in FP64 tables, totals and
+        the CFL reduction in FP64; ``"fp32-geom64"`` is the same) or
+        ``"fp32-geom32"`` (the same march with the geometry, computed in FP64,
+        stored in FP32: less traffic, slightly larger error).
     """
 
     SUBSTEP_RUN = 2
@@ -54,6 +62,9 @@ class EulerCore:
         if precision not in PRECISIONS:
             raise ValueError("EulerCore: precision must be one of %s" %
                              sorted(PRECISIONS))
+        if not hasattr(mesh, "handle"):
+            from .mesh import StaticMesh
+            mesh = StaticMesh.from_mesh(mesh)
         h = ctypes.c_void_p()
         check(lib.scg_euler_create(mesh.handle, float(time_increment),
                                    PRECISIONS[precision], ctypes.byref(h)))

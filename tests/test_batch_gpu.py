@@ -44,7 +44,8 @@ def _cores(ndim, precision, seeds, dt_scale=1.0):
 
 
 @pytest.mark.parametrize("ndim,precision", [(2, "fp64"), (2, "fp32"),
-                                            (3, "fp64"), (3, "fp32")])
+                                            (2, "fp32-geom32"), (3, "fp64"),
+                                            (3, "fp32"), (3, "fp32-geom32")])
 def test_batch_equals_individual_marches(ndim, precision):
     from solvcon_gb300.batch import EulerBatch
     seeds = [3, 11, 17, 29, 41]

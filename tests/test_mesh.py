@@ -126,3 +126,85 @@ def test_mesh_matches_reference_library(seed):
         for name in INT_ARRAYS + REAL_ARRAYS:
             got = np.asarray(getattr(m, name).ndarray).ravel()
             assert np.array_equal(got, r.array(name)), name
+
+
+class _ForeignMesh:
+    """A mesh built by other code, with the reference StaticMesh surface:
+    size properties and whole-buffer tables (ghost rows first) whose
+    ``.ndarray`` is a numpy array, as the reference's pybind11 wrapper
+    exposes them (wrap_StaticMesh.cpp:61-181)."""
+
+    class _Arr:
+        def __init__(self, a):
+            self.ndarray = a
+
+    class _Bc:
+        def __init__(self, name, facn):
+            self.name = name
+            self.facn = _ForeignMesh._Arr(facn)
+
+    def __init__(self, sizes, tables, bcs=()):
+        for k, v in zip(SIZES, sizes):
+            setattr(self, k, int(v))
+        for k, v in tables.items():
+            setattr(self, k, self._Arr(v))
+        self.bcs = [self._Bc(n, f) for n, f in bcs]
+
+
+def _foreign_from_golden(g):
+    s = [int(x) for x in g["sizes"]]
+    tables = {k: g[k] for k in INT_ARRAYS + REAL_ARRAYS + ("clnds",)}
+    # The fixtures carry no clgrp; the reference fills it with -1 (no group).
+    tables["clgrp"] = np.full(s[7] + s[3], -1, dtype="int32")
+    return _ForeignMesh(s, tables, [("walls", np.arange(s[4] * 3,
+                                                        dtype="int32"))])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_from_mesh_takes_reference_tables_verbatim(case):
+    """StaticMesh.from_mesh on a mesh the reference built (its golden
+    tables behind the reference's surface): every table and size comes over
+    unchanged, boundary groups included."""
+    from solvcon_gb300 import StaticMesh
+    g = golden("mesh_" + case)
+    foreign = _foreign_from_golden(g)
+    m = StaticMesh.from_mesh(foreign)
+    _same_as_golden(m, g)
+    np.testing.assert_array_equal(np.asarray(m.clnds.ndarray).ravel(),
+                                  g["clnds"])
+    assert [b.name for b in m.bcs] == ["walls"]
+    np.testing.assert_array_equal(m.bcs[0].facn.ndarray.ravel(),
+                                  np.arange(int(g["sizes"][4]) * 3))
+
+
+def test_from_mesh_rejects_short_tables():
+    from solvcon_gb300 import StaticMesh
+    g = golden("mesh_tri12")
+    foreign = _foreign_from_golden(g)
+    foreign.fccls = _ForeignMesh._Arr(g["fccls"][:-4])
+    with pytest.raises(ValueError, match="fccls"):
+        StaticMesh.from_mesh(foreign)
+
+
+def test_from_mesh_of_the_live_reference_library():
+    """A mesh built by the reference library itself (where it is built
+    here) taken over by StaticMesh.from_mesh equals the host builder's."""
+    from oracle import refbind as rb
+    if not rb.available():
+        pytest.skip("reference library not built on this host")
+    from solvcon_gb300 import StaticMesh, meshgen
+    x, t, c = meshgen.tet_cube(3, 0.15, seed=17)
+    r = rb.RefMesh(3, x, t, c)
+    s = r.sizes()
+    foreign = _ForeignMesh([s[k] for k in SIZES],
+                           {k: r.array(k) for k in INT_ARRAYS + REAL_ARRAYS +
+                            ("clnds", "clgrp")})
+    m = StaticMesh.from_mesh(foreign)
+    assert m.nedge == s["nedge"] > 0
+    np.testing.assert_array_equal(np.asarray(m.ednds.ndarray).ravel(),
+                                  r.array("ednds"))
+    # build_mesh builds no edges; every other table is compared.
+    ours = meshgen.build_mesh(3, x, t, c)
+    for k in set(INT_ARRAYS + REAL_ARRAYS) - {"ednds"}:
+        np.testing.assert_array_equal(np.asarray(getattr(m, k).ndarray),
+                                      np.asarray(getattr(ours, k).ndarray), k)
