@@ -416,6 +416,11 @@ int scg_st_stream(const scg_st * solver, void ** out);
  * plumbing of this library).
  * ---------------------------------------------------------------------- */
 
+/* Not in the reference: round n FP64 values to FP32 on the device exactly as
+ * the FP32 march rounds its FP64 geometry tables where it uses them
+ * (round to nearest even, formed on the integer pipe), for checking that
+ * rounding.  Synchronous; allocates its own device buffers. */
+int scg_geometry_round(const double * in, float * out, int64_t n);
 /* Device FMA throughput in TFLOP/s for SCG_FP64 or SCG_FP32 (a register-only
  * FMA chain over all SMs, iters FMAs-per-accumulator). */
 int scg_fma_peak(int precision, int iters, double * tflops);

@@ -1693,3 +1693,40 @@ std::unique_ptr<EulerCoreBase> make_euler_core(HostMesh const & mesh, double dt,
 }
 
 } // namespace scg
+
+namespace
+{
+
+// One FP64 geometry value per thread, rounded as the FP32 march rounds it.
+__global__ void k_geo_round(double const * in, float * out, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        out[i] = scg::dev::geo_r<float>(in[i]);
+    }
+}
+
+} // namespace
+
+extern "C" int scg_geometry_round(const double * in, float * out, int64_t n)
+{
+    return scg::guarded([&] {
+        if (n < 0 || (n > 0 && (!in || !out)))
+        {
+            throw std::invalid_argument("scg_geometry_round: null buffer or negative count");
+        }
+        if (n == 0)
+        {
+            return;
+        }
+        scg::DevBuf<double> din(static_cast<size_t>(n));
+        scg::DevBuf<float> dout(static_cast<size_t>(n));
+        scg::cuda_check(cudaMemcpy(din.ptr, in, din.bytes(), cudaMemcpyHostToDevice), "H2D");
+        int const block = 256;
+        int64_t const grid = (n + block - 1) / block;
+        k_geo_round<<<static_cast<unsigned>(grid), block>>>(din.ptr, dout.ptr, n);
+        scg::launched(nullptr, "geometry_round");
+        scg::cuda_check(cudaMemcpy(out, dout.ptr, dout.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    });
+}

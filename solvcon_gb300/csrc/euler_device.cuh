@@ -115,6 +115,42 @@ struct Tiny<float>
     static constexpr float AZ = 1.e-37f;
 };
 
+// A geometry value (stored G) in the march's precision R.  FP64 geometry read
+// by the FP32 march is rounded to nearest even on the integer pipe: a
+// double -> float conversion instruction issues on the FP64 pipe, which on
+// GB300 runs at a small fraction of the FP32 rate, and the FP32 march
+// converts ~60 geometry values per cell-substep.  For an FP64 value in the
+// range of normal floats the result is the IEEE round-to-nearest-even
+// float: the exponent is rebiased by 1023 - 127 = 896 in the top bits of the
+// 32-bit word formed from the sign-less high word shifted left by 3 and the
+// top 3 bits of the low word (the top mantissa bits land in place, and the
+// exponent's lost high bits cancel modulo 2^32), then the 29 dropped mantissa
+// bits round it (above half up, exactly half to even).  Zero, FP32
+// subnormals, overflow, inf and NaN take the conversion instruction.
+template <typename R, typename G>
+__device__ __forceinline__ R geo_r(G v)
+{
+    if constexpr (sizeof(R) == 4 && sizeof(G) == 8)
+    {
+        unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
+        unsigned const hi = static_cast<unsigned>(b >> 32);
+        unsigned const lo = static_cast<unsigned>(b);
+        unsigned const e = (hi >> 20) & 0x7FFu;
+        if (e - 897u >= 254u) // biased exponent outside [897, 1150]
+        {
+            return __double2float_rn(v);
+        }
+        unsigned r = ((hi << 3) | (lo >> 29)) - 0xC0000000u;
+        unsigned const rem = lo & 0x1FFFFFFFu;
+        r += static_cast<unsigned>(rem > 0x10000000u) | (static_cast<unsigned>(rem == 0x10000000u) & r);
+        return __uint_as_float(r | (hi & 0x80000000u));
+    }
+    else
+    {
+        return R(v);
+    }
+}
+
 // Reciprocal square root: the library routine for each precision.
 __device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
 __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }

@@ -120,7 +120,7 @@ __device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0
 template <int ND, typename R, typename G>
 __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t icl)
 {
-    return R(ldg(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
+    return geo_r<R>(ldg(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
 }
 
 // What calc_soln hands to calc_dsoln of the same cell when the neighbour
@@ -329,7 +329,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
             acc[i].add(-fl[i]);
         }
     }
-    R const ivol = R(ldg(a.cgeo + 0 * a.ncell + icl));
+    R const ivol = geo_r<R>(ldg(a.cgeo + 0 * a.ncell + icl));
 #pragma unroll
     for (int i = 0; i < NEQ; ++i)
     {
@@ -371,7 +371,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     R const pr = ga1 * (so0n[NEQ - 1] - ke);
     R const pra = (pr + fabs(pr)) / R(2);
     R const wspd = sqr_t(ga * pra * ri) + sqr_t(momsq) * ri;
-    R const cflo = wspd * R(ldg(a.cgeo + 1 * a.ncell + icl));
+    R const cflo = wspd * geo_r<R>(ldg(a.cgeo + 1 * a.ncell + icl));
     // pra / (pra + TINY) is exactly 1 whenever TINY does not change pra (any
     // pressure above ~1e-44 in FP64), so the division is taken only below.
     R const prt = pra + Tiny<R>::CFL;

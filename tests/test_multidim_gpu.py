@@ -610,3 +610,33 @@ def test_core_on_a_reference_built_mesh():
         ec.march(int(g["steps"]))
         for a in ("so0n", "so1n", "cflo"):
             assert_rel(getattr(ec, a).ndarray, g[a], 1e-10, case + " " + a)
+
+
+def test_geometry_rounding_is_round_to_nearest_even():
+    """The FP32 march rounds its FP64 geometry tables to FP32 on the integer
+    pipe; on the device that rounding equals IEEE round-to-nearest-even
+    (numpy's float64 -> float32) bit for bit: random values across the FP32
+    range, exact ties, near-ties, mantissa carries into the exponent, and
+    the values that take the conversion instruction (zero, FP32 subnormals,
+    overflow, inf, NaN)."""
+    from solvcon_gb300._lib import check, lib, ptr
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    bits = rng.integers(0, 2 ** 63, n, dtype=np.uint64)
+    bits |= rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    exp = rng.integers(860, 1190, n, dtype=np.uint64)
+    bits = (bits & ~np.uint64(0x7FF << 52)) | (exp << np.uint64(52))
+    low = np.uint64(0x1FFFFFFF)
+    for k, pat in enumerate((0x10000000, 0x0FFFFFFF, 0x10000001)):
+        sl = slice(k * 50000, (k + 1) * 50000)
+        bits[sl] = (bits[sl] & ~low) | np.uint64(pat)
+    bits[200000:250000] |= np.uint64((1 << 52) - 1)
+    x = bits.view(np.float64).copy()
+    x[:8] = [0.0, -0.0, 1e-40, -3e-39, 1e39, np.inf, -np.inf, np.nan]
+    got = np.empty(n, dtype=np.float32)
+    check(lib.scg_geometry_round(ptr(x), ptr(got), n))
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32)
+    g, w = got.view(np.uint32), want.view(np.uint32)
+    same = (g == w) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), x[~same][:5]
