@@ -264,11 +264,27 @@ def time_e2e(core, steps):
     return (t1 - t0) * 1e3, h2d, d2h
 
 
+_SYNTH = None
+
+
+def synth():
+    """The workload generators (solvcon_gb300/synth.py, plain numpy), loaded
+    by path: the CPU arms build their samples without importing the package
+    and its native library."""
+    global _SYNTH
+    if _SYNTH is None:
+        import importlib.util
+        path = os.path.join(ROOT, "solvcon_gb300", "synth.py")
+        spec = importlib.util.spec_from_file_location("_scg_synth", path)
+        _SYNTH = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(_SYNTH)
+    return _SYNTH
+
+
 def tube_state(ncoord, seed):
     """The 1D workload: a Sod-type tube on [-1, 1] (random left/right
     density and pressure, at rest), its dt for CFL 0.8."""
-    from solvcon_gb300.serving import sod_tube_state
-    return sod_tube_state(ncoord, seed)
+    return synth().sod_tube_state(ncoord, seed)
 
 
 def scalar_state(ncelm):
@@ -284,8 +300,11 @@ def scalar_state(ncelm):
 
 def _oracle_setup(workload, size, seed_offset):
     """One seeded sample of a workload on the CPU oracle: returns (units per
-    step, march(steps))."""
+    step, march(steps)).  The sample (grid, mesh and state) is built with
+    the plain-numpy generators and the oracle's own mesh build, so nothing
+    of the GPU library is loaded."""
     from oracle import oracle as ora
+    sy = synth()
     if workload == "tube1d":
         x, so0, dt = tube_state(size, 2026 + seed_offset)
         o = ora.OracleEuler1D(size, dt)
@@ -294,14 +313,20 @@ def _oracle_setup(workload, size, seed_offset):
         o.setup_march()
         return size, lambda k: o.march_alpha(2, k)
     if workload == "spacetime":
-        grid, so0, so1, dt = scalar_state(size)
-        o = ora.OracleSpacetime(0, grid.xcoord, dt)
-        o.so0[:] = so0
-        o.so1[:] = so1
+        x = sy.grid_xcoord(sy.grid_xloc(0.0, 2.0 * np.pi, int(size)))
+        o = ora.OracleSpacetime(0, x, 0.8 * (2.0 * np.pi / size))
+        o.so0[:] = np.sin(x)
+        o.so1[:] = np.cos(x)
         o.setup_march()
-        return grid.xsize - 4, lambda k: o.march_alpha(2, k)
-    w, mesh, state, faces = make_workload(workload, nside=size,
-                                          seed_offset=seed_offset)
+        return x.size - 4, lambda k: o.march_alpha(2, k)
+    w = dict(WORKLOADS[workload])
+    seed = w["seed"] + seed_offset
+    gen = sy.tri_square if w["ndim"] == 2 else sy.tet_cube
+    mesh = ora.OracleMesh(w["ndim"], *gen(size, w["jitter"], seed))
+    clcnd = mesh.clcnd[mesh.ngstcell:]
+    state = sy.quadrant_state(clcnd, seed=seed) if w["ndim"] == 2 else \
+        sy.blast_state(clcnd)
+    faces = mesh.bndfcs[:, 0]
     o = ora.OracleEuler(mesh, 1e-4)
     o.init_solution(1.4, 1.0, [0.0] * mesh.ndim, 1.0)
     o.so0n[o.ngstcell:] = state

@@ -105,6 +105,25 @@ typedef struct
 void ora_st_setup(ora_st * s);
 void ora_st_march(ora_st * s, int alpha, int64_t steps);
 
+/* A StaticMesh built on the CPU (mesh_oracle.c): every table whole, ghost
+ * rows first, in the reference's layout (StaticMesh.hpp:434-451); widths
+ * ndim for ndcrd/fccnd/fcnml/clcnd, 5 fcnds, 4 fccls, 9 clnds, 7 clfcs,
+ * 3 bndfcs, 1 for the rest. */
+typedef struct
+{
+    int32_t ndim;
+    int64_t nnode, nface, ncell, nbound, ngstnode, ngstface, ngstcell;
+    double *ndcrd, *fccnd, *fcnml, *fcara, *clcnd, *clvol;
+    int32_t *fctpn, *cltpn, *clgrp, *fcnds, *fccls, *clnds, *clfcs, *bndfcs;
+} ora_built_mesh;
+
+/* build_interior (with metrics), build_boundary (no named groups) and
+ * build_ghost of a mesh of ncell cells: cltpn[ncell], clnds[ncell][9].
+ * Returns 0, or -1 (bad ndim, out of memory).  Free with ora_mesh_free. */
+int ora_mesh_build(int ndim, int64_t nnode, int64_t ncell, const double * ndcrd, const int32_t * cltpn,
+                   const int32_t * clnds, ora_built_mesh * out);
+void ora_mesh_free(ora_built_mesh * m);
+
 #ifdef __cplusplus
 }
 #endif

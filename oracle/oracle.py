@@ -88,12 +88,84 @@ class _OraEuler(ctypes.Structure):
 def mesh_tables(mesh):
     """Whole-buffer copies of the tables the march reads, plus sizes, from
     any object with the StaticMesh surface."""
-    t = {n: np.ascontiguousarray(np.array(getattr(mesh, n).ndarray))
+    t = {n: np.ascontiguousarray(np.array(getattr(getattr(mesh, n), "ndarray",
+                                                  getattr(mesh, n))))
          for n in MESH_NAMES}
     sizes = {k: int(getattr(mesh, k)) for k in
              ("ndim", "nnode", "nface", "ncell", "ngstnode", "ngstface",
               "ngstcell")}
     return t, sizes
+
+
+class _OraBuilt(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int32)] + \
+        [(k, ctypes.c_int64) for k in ("nnode", "nface", "ncell", "nbound",
+                                       "ngstnode", "ngstface", "ngstcell")] + \
+        [(k, _P) for k in ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd",
+                           "clvol", "fctpn", "cltpn", "clgrp", "fcnds",
+                           "fccls", "clnds", "clfcs", "bndfcs")]
+
+
+class OracleMesh:
+    """A mesh built by the oracle's own restatement of the reference's
+    StaticMesh build (oracle/mesh_oracle.c): build_interior with metrics,
+    build_boundary with every boundary face in one group, build_ghost.
+
+    ``OracleMesh(ndim, ndcrd, cltpn, clnds)`` (clnds as [ncell, 1 + nodes]
+    rows, count first).  The sizes are attributes and every table is a whole
+    numpy array with its ghost rows first, in the reference's shapes, so
+    :class:`OracleEuler` runs on it directly.  The GPU library is not used.
+    """
+
+    WIDTHS = {"fcara": 0, "clvol": 0, "fctpn": 0, "cltpn": 0, "clgrp": 0,
+              "fcnds": 5, "fccls": 4, "clnds": 9, "clfcs": 7, "bndfcs": 3}
+
+    def __init__(self, ndim, ndcrd, cltpn, clnds):
+        ndcrd = np.ascontiguousarray(ndcrd, dtype="float64")
+        cltpn = np.ascontiguousarray(cltpn, dtype="int32")
+        full = np.full((len(cltpn), 9), -1, dtype="int32")
+        c = np.asarray(clnds, dtype="int32")
+        full[:, :c.shape[1]] = c
+        out = _OraBuilt()
+        L = lib()
+        L.ora_mesh_build.argtypes = [ctypes.c_int, ctypes.c_int64,
+                                     ctypes.c_int64, _P, _P, _P, _P]
+        L.ora_mesh_free.argtypes = [_P]
+        rc = L.ora_mesh_build(int(ndim), ndcrd.shape[0], cltpn.size,
+                              ndcrd.ctypes.data, cltpn.ctypes.data,
+                              full.ctypes.data, ctypes.byref(out))
+        if rc != 0:
+            raise ValueError("ora_mesh_build failed")
+        try:
+            self.ndim = int(out.ndim)
+            for k in ("nnode", "nface", "ncell", "nbound", "ngstnode",
+                      "ngstface", "ngstcell"):
+                setattr(self, k, int(getattr(out, k)))
+            rows = {"node": self.ngstnode + self.nnode,
+                    "face": self.ngstface + self.nface,
+                    "cell": self.ngstcell + self.ncell}
+            kind = {"ndcrd": "node", "fccnd": "face", "fcnml": "face",
+                    "fcara": "face", "clcnd": "cell", "clvol": "cell",
+                    "fctpn": "face", "cltpn": "cell", "clgrp": "cell",
+                    "fcnds": "face", "fccls": "face", "clnds": "cell",
+                    "clfcs": "cell"}
+            for name, _ in _OraBuilt._fields_[8:]:
+                n = self.nbound if name == "bndfcs" else rows[kind[name]]
+                w = self.WIDTHS.get(name, self.ndim)
+                real = name in ("ndcrd", "fccnd", "fcnml", "fcara", "clcnd",
+                                "clvol")
+                ctype = ctypes.c_double if real else ctypes.c_int32
+                size = n * max(w, 1)
+                buf = np.ctypeslib.as_array(
+                    (ctype * max(size, 1)).from_address(getattr(out, name)))
+                arr = np.array(buf[:size])
+                setattr(self, name, arr.reshape((n, w)) if w else arr)
+        finally:
+            L.ora_mesh_free(ctypes.byref(out))
+
+    @property
+    def boundary_faces(self):
+        return self.bndfcs[:, 0].copy()
 
 
 class OracleEuler:

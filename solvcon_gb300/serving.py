@@ -30,6 +30,7 @@ from .batch import EulerBatch
 from .multidim import EulerCore
 from .onedim import Euler1DCore, lib as lib1d
 from ._lib import check
+from .synth import sod_tube_state, tube_dt
 
 __all__ = ["Request", "Server", "poisson_arrivals", "sod_tube_state"]
 
@@ -61,27 +62,6 @@ class Request:
 def poisson_arrivals(rate, n, seed=0):
     rng = np.random.Generator(np.random.PCG64(seed))
     return np.cumsum(rng.exponential(1.0 / rate, n))
-
-
-def sod_tube_state(ncoord, seed):
-    """A Sod-type tube on [-1, 1]: random left/right (rho, p), at rest."""
-    rng = np.random.Generator(np.random.PCG64(seed))
-    rl, rr = rng.uniform(0.5, 1.5), rng.uniform(0.1, 0.5)
-    pl, pr = rng.uniform(0.5, 1.5), rng.uniform(0.05, 0.3)
-    x = np.linspace(-1.0, 1.0, ncoord)
-    so0 = np.zeros((ncoord, 3))
-    left = x < 0.0
-    so0[:, 0] = np.where(left, rl, rr)
-    so0[:, 2] = np.where(left, pl, pr) / 0.4
-    return x, so0, tube_dt(ncoord)
-
-
-def tube_dt(ncoord):
-    """dt of a tube: CFL 0.8 for the largest wave speed the random states
-    can produce (acoustic speed <= 2.05, post-shock |u| + c below 4.5), so
-    it depends on the size only and a tube slot serves every request of its
-    size."""
-    return 0.8 * (2.0 / (ncoord - 1)) / 4.5
 
 
 # Tube sizes served: 16 log-spaced odd sizes over [1k, 100k] points.

@@ -17,6 +17,7 @@ import numpy as np
 from . import _lib
 from ._lib import check, ptr
 from .buffer import SimpleArray
+from .synth import ST_BOUND_COUNT as BOUND_COUNT, grid_xcoord, grid_xloc
 
 __all__ = ["Grid", "LinearScalarSolver", "InviscidBurgersSolver"]
 
@@ -35,7 +36,6 @@ lib = _lib.bind_more({
     "scg_st_stream": ([_vp, _vp], ctypes.c_int),
 })
 
-BOUND_COUNT = 2
 
 
 class Grid:
@@ -53,12 +53,7 @@ class Grid:
                 raise ValueError("Grid::Grid(xmin=%g, xmax=%g, ncelm=%d) "
                                  "invalid arguments: xmin >= xmax"
                                  % (xmin, xmax, ncelm))
-            space = (xmax - xmin) / ncelm
-            xloc = np.empty(ncelm + 1)
-            xloc[0] = xmin
-            for it in range(1, ncelm):
-                xloc[it] = xloc[it - 1] + space
-            xloc[ncelm] = xmax
+            xloc = grid_xloc(xmin, xmax, ncelm)
         elif len(args) == 1:
             xloc = np.asarray(args[0], dtype="float64")
         else:
@@ -75,18 +70,7 @@ class Grid:
         self.ncelm = xloc.size - 1
         self.xmin = float(xloc[0])
         self.xmax = float(xloc[-1])
-        nx = self.ncelm * 2 + 1 + BOUND_COUNT * 2
-        x = np.zeros(nx)
-        x[BOUND_COUNT:BOUND_COUNT + 2 * xloc.size - 1:2] = xloc
-        for it in range(self.ncelm):
-            ref = it * 2 + BOUND_COUNT + 1
-            x[ref] = (x[ref - 1] + x[ref + 1]) / 2
-        for it in range(1, BOUND_COUNT + 1):
-            ref = BOUND_COUNT
-            x[ref - it] = x[ref] + x[ref] - x[ref + it]
-            ref = nx - BOUND_COUNT - 1
-            x[ref + it] = x[ref] + x[ref] - x[ref - it]
-        self.xcoord = x
+        self.xcoord = grid_xcoord(xloc)
 
     @property
     def nselm(self):

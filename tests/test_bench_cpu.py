@@ -89,3 +89,43 @@ def test_pin_device_one_gpu_per_rank(monkeypatch):
     monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "5")
     bench.pin_device(0)
     assert os.environ["CUDA_VISIBLE_DEVICES"] == "5"
+
+
+def test_cpu_arm_loads_nothing_of_the_library():
+    """The CPU arms build their samples with the plain-numpy generators and
+    the oracle's own mesh build: neither the package nor libscg.so is
+    loaded in the process that marches."""
+    code = (
+        "import sys, numpy as np\n"
+        "sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "for wl, n in (('tri2d', 12), ('tet3d', 3), ('tube1d', 101),\n"
+        "              ('spacetime', 64)):\n"
+        "    units, march = bench._oracle_setup(wl, n, 0)\n"
+        "    march(1)\n"
+        "assert not [m for m in sys.modules if m.startswith('solvcon_gb300')]\n"
+        "assert 'libscg' not in open('/proc/self/maps').read()\n"
+        "print('ok')\n" % ROOT)
+    run = subprocess.run([sys.executable, "-c", code], cwd=ROOT,
+                         capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0 and "ok" in run.stdout, run.stderr[-2000:]
+
+
+def test_cpu_sample_equals_the_gpu_workload_sample():
+    """The CPU arm's sample of the 2D workload is the GPU arm's workload at
+    the same size and seed: same mesh tables, same state."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    from oracle import oracle as ora
+    w, mesh, state, faces = bench.make_workload("tri2d", nside=20,
+                                                seed_offset=3)
+    sy = bench.synth()
+    m = ora.OracleMesh(2, *sy.tri_square(20, w["jitter"], w["seed"] + 3))
+    for name in ("fcnds", "fccls", "clfcs", "clcnd", "clvol", "ndcrd"):
+        np.testing.assert_array_equal(
+            np.asarray(getattr(m, name)).ravel(),
+            np.asarray(getattr(mesh, name).ndarray).ravel(), name)
+    np.testing.assert_array_equal(
+        sy.quadrant_state(m.clcnd[m.ngstcell:], seed=w["seed"] + 3), state)
+    np.testing.assert_array_equal(m.bndfcs[:, 0], faces)

@@ -209,3 +209,71 @@ def test_oracle_spacetime_against_reference_library():
                     np.testing.assert_array_equal(getattr(o, a), ref.get(a),
                                                   "%d %d %s" % (kind, alpha,
                                                                 a))
+
+
+MESH_CASES = ("tri3", "quad1", "mixed", "tet1", "hex1", "prism1", "pyr1",
+              "tri12", "quad8", "tet3")
+MESH_TABLES = ("fctpn", "cltpn", "fcnds", "fccls", "clfcs", "bndfcs",
+               "ndcrd", "fccnd", "fcnml", "fcara", "clcnd", "clvol")
+
+
+def _oracle_mesh_equals(m, tables, sizes, clnds_full=None):
+    got = [m.ndim, m.nnode, m.nface, m.ncell, m.nbound, m.ngstnode,
+           m.ngstface, m.ngstcell]
+    assert got == [int(x) for x in sizes[:8]]
+    for name in MESH_TABLES:
+        np.testing.assert_array_equal(np.asarray(getattr(m, name)).ravel(),
+                                      np.asarray(tables[name]).ravel(), name)
+    want = np.asarray(tables["clnds"]).reshape(m.clnds.shape)
+    for row in range(want.shape[0]):
+        n = want[row, 0]
+        assert np.array_equal(m.clnds[row, :n + 1], want[row, :n + 1]), row
+
+
+@pytest.mark.parametrize("case", MESH_CASES)
+def test_oracle_mesh_matches_reference_golden(case):
+    """The oracle's own StaticMesh build (oracle/mesh_oracle.c) gives the
+    reference's tables entry for entry: interior, boundary and ghost."""
+    from oracle import oracle as ora
+    g = golden("mesh_" + case)
+    m = ora.OracleMesh(int(g["ndim"]), g["ndcrd_in"], g["cltpn_in"],
+                       g["clnds_in"])
+    _oracle_mesh_equals(m, g, g["sizes"])
+
+
+def test_oracle_mesh_against_reference_library():
+    from oracle import oracle as ora
+    from oracle import refbind as rb
+    if not rb.available():
+        pytest.skip("reference library not built on this host")
+    from solvcon_gb300 import synth
+    for nd, (x, t, c) in ((2, synth.tri_square(30, 0.2, 8)),
+                          (2, synth.quad_square(11, 0.15, 8)),
+                          (3, synth.tet_cube(5, 0.15, 8)),
+                          (3, synth.hex_cube(4, 0.1, 8)),
+                          (3, synth.prism_slab(5, 3, 0.1, 8))):
+        r = rb.RefMesh(nd, x, t, c)
+        s = r.sizes()
+        m = ora.OracleMesh(nd, x, t, c)
+        _oracle_mesh_equals(m, {k: r.array(k) for k in MESH_TABLES +
+                                ("clnds",)},
+                            [s[k] for k in ("ndim", "nnode", "nface", "ncell",
+                                            "nbound", "ngstnode", "ngstface",
+                                            "ngstcell")])
+
+
+def test_oracle_mesh_equals_the_library_mesh_builder():
+    """The two restatements of the mesh build -- the oracle's in C and the
+    library's host builder -- agree table for table on the workloads'
+    generators, so a march on either mesh is the same march."""
+    from oracle import oracle as ora
+    from solvcon_gb300 import meshgen
+    for nd, (x, t, c) in ((2, meshgen.tri_square(40, 0.2, 3)),
+                          (3, meshgen.tet_cube(5, 0.15, 3))):
+        m = ora.OracleMesh(nd, x, t, c)
+        lib_mesh = meshgen.build_mesh(nd, x, t, c)
+        tables = {k: np.asarray(getattr(lib_mesh, k).ndarray)
+                  for k in MESH_TABLES + ("clnds",)}
+        _oracle_mesh_equals(m, tables, [getattr(lib_mesh, k) for k in (
+            "ndim", "nnode", "nface", "ncell", "nbound", "ngstnode",
+            "ngstface", "ngstcell")])
