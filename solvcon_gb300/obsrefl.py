@@ -47,8 +47,10 @@ class ObliqueShockMesher:
         return ((self.x1 - self.x0) / self.nx, (self.y1 - self.y0) / self.ny)
 
     def _xy(self, it, jt):
-        dx, dy = self.cell_extent
-        return (self.x0 + it * dx, self.y0 + jt * dy)
+        # The reference's expression (_driver.py:45-47), so that the points,
+        # and the triangulation built on them, are the same to the last bit.
+        return (self.x0 + it * (self.x1 - self.x0) / self.nx,
+                self.y0 + jt * (self.y1 - self.y0) / self.ny)
 
     def _grid_nodes(self):
         return [self._xy(it, jt) for jt in range(self.ny + 1)

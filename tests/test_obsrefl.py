@@ -160,3 +160,33 @@ def test_driver_reaches_the_analytic_zones():
         assert near.sum() >= 3
         assert abs(rho[near].mean() / z[0] - 1) < tol, (x, y)
         assert abs(p[near].mean() / z[3] - 1) < tol, (x, y)
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 16), (24, 6)])
+def test_unstructured_mesh_is_the_references(nx, ny):
+    """The unstructured flavor triangulates exactly the reference mesher's
+    points into exactly its triangles (fixtures made by running the
+    reference's ObliqueShockMesher, _driver.py:127-260): the same scattered
+    points bit for bit, the same corner-ear Steiner points, the same
+    triangle set.  Only the numbering differs where the reference's follows
+    its Bowyer-Watson insertion order: the Steiner points are appended, and
+    the cells listed, in another order."""
+    from _util import golden
+    from solvcon_gb300.obsrefl import ObliqueShockMesher
+    g = golden("obsrefl_%dx%d" % (nx, ny))
+    m = ObliqueShockMesher(nx=nx, ny=ny)
+    pts, tris = m._triangulate(m._scattered_nodes())
+    ours = np.asarray(pts, dtype="float64")
+    ref = g["points"]
+    assert ours.shape == ref.shape
+    index = {tuple(p): k for k, p in enumerate(ref.tolist())}
+    to_ref = np.array([index[tuple(p)] for p in ours.tolist()])
+    assert sorted(to_ref.tolist()) == list(range(len(ref)))
+
+    def canon(t):
+        t = list(t)
+        k = t.index(min(t))
+        return tuple(t[k:] + t[:k])
+    mapped = {canon(to_ref[list(t)]) for t in tris}
+    assert mapped == {canon(t) for t in g["triangles"].tolist()}
+    assert len(tris) == len(g["triangles"])
