@@ -80,7 +80,7 @@ constexpr int batch_min_blocks()
     }
     else
     {
-        return scg::dev::min_blocks<ND, R, CT1, B>();
+        return scg::dev::min_blocks<ND, R, CT1, B, G>();
     }
 }
 

@@ -1349,7 +1349,7 @@ public:
         constexpr int SIMPLEX = (ND == 2) ? CT_TRIANGLE : CT_TET;
         if (single_ct == SIMPLEX)
         {
-            constexpr int MINB = min_blocks<ND, R, SIMPLEX, BLOCK>();
+            constexpr int MINB = min_blocks<ND, R, SIMPLEX, BLOCK, G>();
             if constexpr (MINB > 0)
             {
                 k_fused_mb<ND, R, G, SIMPLEX, MINB><<<grid_for(nrow), BLOCK, 0, stream>>>(args());

@@ -116,17 +116,20 @@ struct Tiny<float>
 };
 
 // A geometry value (stored G) in the march's precision R.  FP64 geometry read
-// by the FP32 march is rounded to nearest even on the integer pipe: a
-// double -> float conversion instruction issues on the FP64 pipe, which on
-// GB300 runs at a small fraction of the FP32 rate, and the FP32 march
-// converts ~60 geometry values per cell-substep.  For an FP64 value in the
-// range of normal floats the result is the IEEE round-to-nearest-even
-// float: the exponent is rebiased by 1023 - 127 = 896 in the top bits of the
-// 32-bit word formed from the sign-less high word shifted left by 3 and the
-// top 3 bits of the low word (the top mantissa bits land in place, and the
-// exponent's lost high bits cancel modulo 2^32), then the 29 dropped mantissa
-// bits round it (above half up, exactly half to even).  Zero, FP32
-// subnormals, overflow, inf and NaN take the conversion instruction.
+// by the FP32 march is rounded with integer instructions only: a double ->
+// float conversion instruction issues on the FP64 pipe (16 cycles per warp on
+// GB300, measured), and the FP32 march converts ~60 geometry values per
+// cell-substep, which made that pipe the FP32 march's bottleneck.  In the
+// FP32 normal range the result is IEEE round-to-nearest-even: the word formed
+// by funnel-shifting the sign-less high word left by 3 (taking the low word's
+// top 3 bits) holds the exponent and the top 23 mantissa bits in place, and
+// subtracting (1023 - 127) << 23 modulo 2^32 rebiases the exponent (its
+// high bits shifted out cancel); the 29 dropped bits then round it:
+// (dropped + lsb + 2^28 - 1) >> 29 is 1 exactly when they exceed half, or
+// equal half with an odd lsb.  Values below the FP32 normal range become a
+// signed zero; values beyond it, infinities and NaNs become NaN (no mesh
+// produces them, and a broken table then shows).  Branch-free, so nothing
+// falls back to the conversion instruction.
 template <typename R, typename G>
 __device__ __forceinline__ R geo_r(G v)
 {
@@ -135,14 +138,11 @@ __device__ __forceinline__ R geo_r(G v)
         unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
         unsigned const hi = static_cast<unsigned>(b >> 32);
         unsigned const lo = static_cast<unsigned>(b);
-        unsigned const e = (hi >> 20) & 0x7FFu;
-        if (e - 897u >= 254u) // biased exponent outside [897, 1150]
-        {
-            return __double2float_rn(v);
-        }
-        unsigned r = ((hi << 3) | (lo >> 29)) - 0xC0000000u;
-        unsigned const rem = lo & 0x1FFFFFFFu;
-        r += static_cast<unsigned>(rem > 0x10000000u) | (static_cast<unsigned>(rem == 0x10000000u) & r);
+        unsigned const ahi = hi & 0x7FFFFFFFu;
+        unsigned const e = ahi >> 20;
+        unsigned r = __funnelshift_l(lo, ahi, 3) - 0xC0000000u;
+        r += ((lo & 0x1FFFFFFFu) + (r & 1u) + 0x0FFFFFFFu) >> 29;
+        r = (e - 897u < 254u) ? r : (e > 1150u ? 0x7FC00000u : 0u);
         return __uint_as_float(r | (hi & 0x80000000u));
     }
     else

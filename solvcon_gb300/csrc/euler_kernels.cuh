@@ -150,8 +150,19 @@ __host__ __device__ constexpr bool carries()
 // registers, 80 bytes spilled), 4.66 ms at 4 (128 registers).  With the
 // FP32 delta form (u0, d0 below) 7 blocks stay best in 2D (0.1628 ms; 6:
 // 0.1688, 8: 0.1683) and 4 in 3D (4.80 ms).  The budget per thread (72 /
-// 128 registers) is kept for other block sizes.
-template <int ND, typename R, int CT, int BLOCK>
+// 128 registers) is kept for other block sizes.  With FP64 geometry tables
+// (G = double) the 2D budget is set apart, as its geometry loads and their
+// rounding hold more registers.
+#ifndef SCG_CARRY_REGS_2D
+#define SCG_CARRY_REGS_2D 72
+#endif
+#ifndef SCG_CARRY_REGS_2D_G64
+#define SCG_CARRY_REGS_2D_G64 72
+#endif
+#ifndef SCG_CARRY_REGS_3D
+#define SCG_CARRY_REGS_3D 128
+#endif
+template <int ND, typename R, int CT, int BLOCK, typename G = R>
 __host__ __device__ constexpr int min_blocks()
 {
     if constexpr (!carries<R, CT>())
@@ -160,7 +171,8 @@ __host__ __device__ constexpr int min_blocks()
     }
     else
     {
-        return 65536 / (BLOCK * (ND == 2 ? 72 : 128));
+        constexpr int regs = ND == 3 ? SCG_CARRY_REGS_3D : (sizeof(G) == 8 ? SCG_CARRY_REGS_2D_G64 : SCG_CARRY_REGS_2D);
+        return 65536 / (BLOCK * regs);
     }
 }
 
