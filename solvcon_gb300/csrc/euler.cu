@@ -251,9 +251,43 @@ __global__ void k_init(R * nxt, R * gamma, int64_t ngst, int64_t nrow, double ga
     }
 }
 
+// The FP32 state of a body row is its record's so0 plus the rounding residual
+// the march carries beside it ([NEQ][ncell], see fused_cell); comp is that
+// residual for the so0 table being read or written, else null.
+struct Residual
+{
+    void * comp = nullptr;
+    int64_t ngst = 0, ncell = 0;
+};
+
+// Value k of row r of a record field in FP64, the residual added.
+template <int ND, typename R>
+__device__ __forceinline__ double field_value(R const * rec, int64_t r, int off, int k, Residual c)
+{
+    double v = double(rec[r * Rec<ND, R>::RS + off + k]);
+    if (c.comp && r >= c.ngst)
+    {
+        v += double(static_cast<R const *>(c.comp)[k * c.ncell + (r - c.ngst)]);
+    }
+    return v;
+}
+
+// Store an FP64 value into a record field: the rounded value, and for a body
+// row of an FP32 so0 table the part the rounding dropped into the residual.
+template <int ND, typename R>
+__device__ __forceinline__ void field_store(R * rec, int64_t r, int off, int k, double x, Residual c)
+{
+    R const t = R(x);
+    rec[r * Rec<ND, R>::RS + off + k] = t;
+    if (c.comp && r >= c.ngst)
+    {
+        static_cast<R *>(c.comp)[k * c.ncell + (r - c.ngst)] = R(x - double(t));
+    }
+}
+
 // Record field <-> FP64 reference-layout table.
 template <int ND, typename R>
-__global__ void k_get_field(R const * rec, double * out, int64_t nrow, int off, int width)
+__global__ void k_get_field(R const * rec, double * out, int64_t nrow, int off, int width, Residual c)
 {
     int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (r >= nrow)
@@ -262,12 +296,12 @@ __global__ void k_get_field(R const * rec, double * out, int64_t nrow, int off, 
     }
     for (int k = 0; k < width; ++k)
     {
-        out[r * width + k] = double(rec[r * Rec<ND, R>::RS + off + k]);
+        out[r * width + k] = field_value<ND, R>(rec, r, off, k, c);
     }
 }
 
 template <int ND, typename R>
-__global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, int width)
+__global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, int width, Residual c)
 {
     int64_t const r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (r >= nrow)
@@ -276,7 +310,7 @@ __global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, i
     }
     for (int k = 0; k < width; ++k)
     {
-        rec[r * Rec<ND, R>::RS + off + k] = R(in[r * width + k]);
+        field_store<ND, R>(rec, r, off, k, in[r * width + k], c);
     }
 }
 
@@ -285,7 +319,8 @@ __global__ void k_set_field(R * rec, double const * in, int64_t nrow, int off, i
 // is accessed in contiguous 16-byte pieces (vec: the host table is 16-byte
 // aligned) and the records are gathered on the device.
 template <int ND, typename R>
-__global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int off, int width, bool vec)
+__global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int off, int width, bool vec,
+                                 Residual c)
 {
     int64_t const n = nrow * width;
     int64_t const i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
@@ -295,7 +330,7 @@ __global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int 
     }
     int64_t const r0 = i / width;
     int const k0 = static_cast<int>(i - r0 * width);
-    double const v0 = double(rec[r0 * Rec<ND, R>::RS + off + k0]);
+    double const v0 = field_value<ND, R>(rec, r0, off, k0, c);
     if (i + 1 >= n)
     {
         out[i] = v0;
@@ -303,7 +338,7 @@ __global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int 
     }
     int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
     int const k1 = k0 + 1 < width ? k0 + 1 : 0;
-    double const v1 = double(rec[r1 * Rec<ND, R>::RS + off + k1]);
+    double const v1 = field_value<ND, R>(rec, r1, off, k1, c);
     if (vec)
     {
         *reinterpret_cast<double2 *>(out + i) = make_double2(v0, v1);
@@ -316,7 +351,8 @@ __global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int 
 }
 
 template <int ND, typename R>
-__global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int off, int width, bool vec)
+__global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int off, int width, bool vec,
+                                 Residual c)
 {
     int64_t const n = nrow * width;
     int64_t const i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
@@ -328,7 +364,7 @@ __global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int o
     int const k0 = static_cast<int>(i - r0 * width);
     if (i + 1 >= n)
     {
-        rec[r0 * Rec<ND, R>::RS + off + k0] = R(in[i]);
+        field_store<ND, R>(rec, r0, off, k0, in[i], c);
         return;
     }
     double2 v;
@@ -342,8 +378,8 @@ __global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int o
     }
     int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
     int const k1 = k0 + 1 < width ? k0 + 1 : 0;
-    rec[r0 * Rec<ND, R>::RS + off + k0] = R(v.x);
-    rec[r1 * Rec<ND, R>::RS + off + k1] = R(v.y);
+    field_store<ND, R>(rec, r0, off, k0, v.x, c);
+    field_store<ND, R>(rec, r1, off, k1, v.y, c);
 }
 
 // so1n written from a mapped host table and then calc_solt of each row as
@@ -448,7 +484,7 @@ __global__ void k_from_f64(double const * in, R * out, int64_t n)
 // number |v| / sqrt(gamma p / rho), and the unclamped CFL number cflo.
 template <int ND, typename R>
 __global__ void k_field(R const * nxt, R const * gamma, R const * cflo, int64_t ngst, int64_t ncell, int which,
-                        double * out)
+                        double * out, Residual c)
 {
     int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (icl >= ncell)
@@ -456,16 +492,15 @@ __global__ void k_field(R const * nxt, R const * gamma, R const * cflo, int64_t 
         return;
     }
     int64_t const row = icl + ngst;
-    R const * u = nxt + row * Rec<ND, R>::RS;
-    double const rho = double(u[0]);
+    double const rho = field_value<ND, R>(nxt, row, 0, 0, c);
     double v[ND];
     double vsq = 0.0;
     for (int d = 0; d < ND; ++d)
     {
-        v[d] = double(u[1 + d]) / rho;
+        v[d] = field_value<ND, R>(nxt, row, 0, 1 + d, c) / rho;
         vsq += v[d] * v[d];
     }
-    double const energy = double(u[ND + 1]);
+    double const energy = field_value<ND, R>(nxt, row, 0, ND + 1, c);
     double const ga = double(gamma[row]);
     double r = 0.0;
     switch (which)
@@ -492,7 +527,7 @@ __global__ void k_field(R const * nxt, R const * gamma, R const * cflo, int64_t 
 // warp shuffles across the block), and min/max of cflo.
 template <int ND, typename R>
 __global__ void __launch_bounds__(BLOCK) k_totals(R const * nxt, double const * clvol, R const * cflo, int64_t ngst,
-                                                  int64_t ncell, double * part)
+                                                  int64_t ncell, double * part, Residual cr)
 {
     constexpr int NEQ = ND + 2;
     __shared__ double sh[BLOCK / 32];
@@ -510,7 +545,7 @@ __global__ void __launch_bounds__(BLOCK) k_totals(R const * nxt, double const * 
         double const v = clvol[row];
         for (int i = 0; i < NEQ; ++i)
         {
-            double const y = double(nxt[row * Rec<ND, R>::RS + i]) * v - c[i];
+            double const y = field_value<ND, R>(nxt, row, 0, i, cr) * v - c[i];
             double const t = s[i] + y;
             c[i] = (t - s[i]) - y;
             s[i] = t;
@@ -756,6 +791,12 @@ public:
         cuda_check(cudaMemsetAsync(d_cflo.ptr, 0, d_cflo.bytes(), stream), "memset");
         cuda_check(cudaMemsetAsync(d_cflc.ptr, 0, d_cflc.bytes(), stream), "memset");
         cuda_check(cudaMemsetAsync(d_limiter.ptr, 0, d_limiter.bytes(), stream), "memset");
+        if constexpr (sizeof(R) == 4)
+        {
+            d_comp.alloc(static_cast<size_t>(NEQ) * std::max<int64_t>(ncell, 1));
+            cuda_check(cudaMemsetAsync(d_comp.ptr, 0, d_comp.bytes(), stream), "memset");
+            comp_live = true;
+        }
 
         // Boundary tables.
         d_gkind.alloc(std::max<int64_t>(ngstcell, 1));
@@ -793,7 +834,7 @@ public:
         for (auto const & r : rec)
             b += r.bytes();
         b += d_fgeo.bytes() + d_cgeo.bytes() + d_nbr.bytes() + d_ctype.bytes();
-        b += d_gamma.bytes() + d_cflo.bytes() + d_cflc.bytes();
+        b += d_gamma.bytes() + d_cflo.bytes() + d_cflc.bytes() + d_comp.bytes();
         b += d_ndcrd.bytes() + d_fccnd.bytes() + d_clcnd.bytes() + d_fcnds.bytes() + d_fccls.bytes() +
              d_clfcs.bytes() + d_cltpn.bytes() + d_clvol.bytes();
         for (auto const & c : ce)
@@ -1031,6 +1072,7 @@ public:
         a.limiter = d_limiter.ptr;
         a.out0 = m_deliver_now ? m_deliver[0].dev : nullptr;
         a.out1 = m_deliver_now ? m_deliver[1].dev : nullptr;
+        a.comp = sizeof(R) == 4 ? d_comp.ptr : nullptr;
         a.ncell = ncell;
         a.ngst = ngstcell;
         a.dt = R(time_increment);
@@ -1090,12 +1132,13 @@ public:
             {
                 // Mapped host table: the gather writes it directly.
                 k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
-                    base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                    base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0, so0_residual(which));
                 launched(stream, "get_field_host");
                 sync();
                 return;
             }
-            k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width);
+            k_get_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width,
+                                                                     so0_residual(which));
             launched(stream, "get_field");
         }
         cuda_check(cudaMemcpyAsync(out, tmp, nb, cudaMemcpyDeviceToHost, stream), "D2H");
@@ -1137,7 +1180,8 @@ public:
                 else
                 {
                     k_set_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
-                        base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0);
+                        base, dev, nrow, off, width, reinterpret_cast<uintptr_t>(dev) % 16 == 0,
+                        so0_written(which));
                     launched(stream, "set_field_host");
                     next_valid = false;
                 }
@@ -1164,7 +1208,8 @@ public:
             R * base;
             int off, width;
             field_of(which, base, off, width);
-            k_set_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width);
+            k_set_field<ND, R><<<grid_for(nrow), BLOCK, 0, stream>>>(base, tmp, nrow, off, width,
+                                                                     so0_written(which));
             launched(stream, "set_field");
         }
         next_valid = false;
@@ -1199,6 +1244,7 @@ public:
                                                                  ND == 3 ? rho * v[2] : 0.0, energy);
             launched(stream, "init_solution");
         }
+        comp_live = false;
         next_valid = false;
         sync();
     }
@@ -1235,6 +1281,7 @@ public:
             break;
         case EO_UPDATE:
             cur ^= 1;
+            comp_live = false; // the residual was so0n's, which is now so0c
             break;
         case EO_CALC_SOLT:
             if (nrow > 0)
@@ -1248,6 +1295,7 @@ public:
                 k_soln<ND, R, G><<<grid_for(ncell), BLOCK, 0, stream>>>(args());
                 launched(stream, "calc_soln");
             }
+            comp_live = false;
             next_valid = false;
             break;
         case EO_BC_SOLN:
@@ -1264,6 +1312,7 @@ public:
                 k_cfl<ND, R, G><<<grid_for(ncell), BLOCK, 0, stream>>>(args());
                 launched(stream, "calc_cfl");
             }
+            comp_live = false; // a rewritten energy no longer has its residual
             next_valid = false;
             break;
         case EO_CALC_DSOLN:
@@ -1300,6 +1349,7 @@ public:
             tbuf = 0;
             next_valid = false;
             next_buf = 1;
+            comp_live = false;
             break;
         default:
             throw std::invalid_argument("EulerCore: unknown operation " + std::to_string(which));
@@ -1312,6 +1362,7 @@ public:
     // already leave it in the new current buffer.
     void march_substep()
     {
+        comp_ready();
         cur ^= 1;
         if (next_valid && next_buf == cur)
         {
@@ -1392,8 +1443,8 @@ public:
                     int off, width;
                     field_of(k == 0 ? EA_SO0N : EA_SO1N, base, off, width);
                     int64_t const n = static_cast<int64_t>(d.nbytes / sizeof(double));
-                    k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(base, d.dev, nrow, off,
-                                                                                       width, true);
+                    k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
+                        base, d.dev, nrow, off, width, true, so0_residual(k == 0 ? EA_SO0N : EA_SO1N));
                     launched(stream, "get_field_host");
                 }
             }
@@ -1446,7 +1497,7 @@ public:
         nblk = static_cast<int>(std::min<int64_t>(std::max<int64_t>(grid_for(ncell), 1), 1024));
         DevBuf<double> part(static_cast<size_t>(nblk * (NEQ + 2)));
         k_totals<ND, R><<<nblk, BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_clvol.ptr, d_cflo.ptr, ngstcell, ncell,
-                                                   part.ptr);
+                                                   part.ptr, so0_residual(EA_SO0N));
         launched(stream, "totals");
         std::vector<double> h(static_cast<size_t>(nblk * (NEQ + 2)));
         cuda_check(cudaMemcpyAsync(h.data(), part.ptr, part.bytes(), cudaMemcpyDeviceToHost, stream), "D2H");
@@ -1486,6 +1537,7 @@ public:
     void batch_begin() override
     {
         upload_bc();
+        comp_ready();
         // Exactly what the first substep of march() does before its fused
         // kernel, minus the buffer swap: so0t of the state in rec[cur ^ 1].
         if (!(next_valid && next_buf == (cur ^ 1)) && nrow > 0)
@@ -1539,6 +1591,7 @@ public:
         v.ncell = ncell;
         v.ngstcell = ngstcell;
         v.stream = stream;
+        v.comp = so0_residual(EA_SO0N).comp;
         return v;
     }
 
@@ -1564,7 +1617,7 @@ public:
         }
         double * d = staging(ncell);
         k_field<ND, R><<<grid_for(ncell), BLOCK, 0, stream>>>(rec[cur ^ 1].ptr, d_gamma.ptr, d_cflo.ptr, ngstcell,
-                                                             ncell, which, d);
+                                                             ncell, which, d, so0_residual(EA_SO0N));
         launched(stream, "field");
         cuda_check(cudaMemcpyAsync(out, d, static_cast<size_t>(ncell) * sizeof(double), cudaMemcpyDeviceToHost,
                                    stream),
@@ -1615,6 +1668,48 @@ private:
     DevBuf<int8_t> d_ctype;
     DevBuf<R> rec[2];
     DevBuf<R> d_gamma, d_cflo, d_cflc;
+    // FP32: the rounding residual of so0n's body rows [NEQ][ncell], fed
+    // back into each cell's next value by the march (fused_cell) and added to
+    // so0n wherever so0n is read; valid while comp_live.  Anything other than
+    // a march that changes so0n (or moves it, update()) drops it; the next
+    // march starts it again from zero.
+    DevBuf<R> d_comp;
+    bool comp_live = false;
+
+    Residual so0_residual(int which) const
+    {
+        Residual c;
+        if (sizeof(R) == 4 && comp_live && which == EA_SO0N)
+        {
+            c.comp = d_comp.ptr;
+            c.ngst = ngstcell;
+            c.ncell = ncell;
+        }
+        return c;
+    }
+
+    // A write of a whole so0n table also writes the residual of each value.
+    Residual so0_written(int which)
+    {
+        Residual c;
+        if (sizeof(R) == 4 && which == EA_SO0N)
+        {
+            c.comp = d_comp.ptr;
+            c.ngst = ngstcell;
+            c.ncell = ncell;
+            comp_live = true;
+        }
+        return c;
+    }
+
+    void comp_ready()
+    {
+        if (sizeof(R) == 4 && !comp_live)
+        {
+            cuda_check(cudaMemsetAsync(d_comp.ptr, 0, d_comp.bytes(), stream), "memset");
+            comp_live = true;
+        }
+    }
 
     // Host blocks a march also writes so0n / so1n into (deliver()).
     struct Delivery

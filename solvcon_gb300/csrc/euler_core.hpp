@@ -143,6 +143,7 @@ public:
         double const * clvol; // [ngstcell + ncell]
         int64_t ncell, ngstcell;
         cudaStream_t stream;
+        void const * comp;    // FP32: rounding residual of so0n [neq][ncell], or null
     };
     virtual StateView state_view() = 0;
 

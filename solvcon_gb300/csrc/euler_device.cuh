@@ -434,6 +434,9 @@ struct MarchArgs
     // [nrow][NEQ] and so1n [nrow][NEQ][ND] in FP64, or null.
     double * out0;
     double * out1;
+    // FP32 march: the rounding residual of each body cell's so0 [NEQ][ncell],
+    // fed back into the cell's next value (see fused_cell), or null.
+    R * comp;
     int64_t ncell;
     int64_t ngst;
     R dt, hdt, qdt;

@@ -151,16 +151,20 @@ __host__ __device__ constexpr bool carries()
 // FP32 delta form (u0, d0 below) 7 blocks stay best in 2D (0.1628 ms; 6:
 // 0.1688, 8: 0.1683) and 4 in 3D (4.80 ms).  The budget per thread (72 /
 // 128 registers) is kept for other block sizes.  With FP64 geometry tables
-// (G = double) the 2D budget is set apart, as its geometry loads and their
-// rounding hold more registers.
+// (G = double) the budget is set apart, as the geometry loads and their
+// rounding hold more registers: 2D, 980k triangles, 0.2350 / 0.2364 /
+// 0.2296 / 0.2175 ms per 2M-cell launch at 64 / 72 / 80 / 96 registers.
 #ifndef SCG_CARRY_REGS_2D
 #define SCG_CARRY_REGS_2D 72
 #endif
 #ifndef SCG_CARRY_REGS_2D_G64
-#define SCG_CARRY_REGS_2D_G64 72
+#define SCG_CARRY_REGS_2D_G64 96
 #endif
 #ifndef SCG_CARRY_REGS_3D
 #define SCG_CARRY_REGS_3D 128
+#endif
+#ifndef SCG_CARRY_REGS_3D_G64
+#define SCG_CARRY_REGS_3D_G64 128
 #endif
 template <int ND, typename R, int CT, int BLOCK, typename G = R>
 __host__ __device__ constexpr int min_blocks()
@@ -171,7 +175,8 @@ __host__ __device__ constexpr int min_blocks()
     }
     else
     {
-        constexpr int regs = ND == 3 ? SCG_CARRY_REGS_3D : (sizeof(G) == 8 ? SCG_CARRY_REGS_2D_G64 : SCG_CARRY_REGS_2D);
+        constexpr int regs = ND == 3 ? (sizeof(G) == 8 ? SCG_CARRY_REGS_3D_G64 : SCG_CARRY_REGS_3D)
+                                     : (sizeof(G) == 8 ? SCG_CARRY_REGS_2D_G64 : SCG_CARRY_REGS_2D);
         return 65536 / (BLOCK * regs);
     }
 }
@@ -970,6 +975,36 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     }
     R so0n[NEQ];
     soln_cell<CT, R, G, true>(a, icl, so0n, CARRY ? &carry : nullptr, DELTA ? u0 : nullptr, d0);
+    // FP32 error feedback: what rounding the new so0 to FP32 drops is kept per
+    // cell and equation (comp) and added back to the cell's next new value,
+    // the rounding taken by an exact two-sum (Knuth) so the kept residual is
+    // exactly the part lost.  A CESE cell's new value is formed from its
+    // neighbours' stored values, so without this every substep's FP32
+    // roundings of the whole state are lost to the totals for good, and they
+    // do not average out (measured: the totals of a 3D blast drift ~1e-8 from
+    // FP64's in 200 steps, also with FP64 arithmetic on FP32-rounded states);
+    // with the residual fed back they cancel over the mesh, and the totals stay
+    // within ~1e-10 of FP64's.  Locally the residual re-added is below half an
+    // ulp of the state, the size of the rounding itself.  Neighbours read only
+    // the rounded so0; the API's so0n and the totals are so0 + comp; d0 becomes
+    // the change including the residual.
+    R cnew[NEQ];
+    if constexpr (DELTA)
+    {
+        if (a.comp)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                R const y = d0[i] + a.comp[i * a.ncell + icl];
+                R const t = u0[i] + y;
+                R const yb = t - u0[i];
+                cnew[i] = (u0[i] - (t - yb)) + (y - yb);
+                so0n[i] = t;
+                d0[i] = y;
+            }
+        }
+    }
 
     // Boundary faces: ghost so0n (pre-rewrite), so1n and next so0t.
 #pragma unroll
@@ -1000,6 +1035,18 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     if (DELTA && so0n[NEQ - 1] != e_soln)
     {
         d0[NEQ - 1] = so0n[NEQ - 1] - u0[NEQ - 1]; // calc_cfl rewrote the energy
+        cnew[NEQ - 1] = R(0);                      // ... and nothing was dropped
+    }
+    if constexpr (DELTA)
+    {
+        if (a.comp)
+        {
+#pragma unroll
+            for (int i = 0; i < NEQ; ++i)
+            {
+                a.comp[i * a.ncell + icl] = cnew[i];
+            }
+        }
     }
     if constexpr (CARRY)
     {

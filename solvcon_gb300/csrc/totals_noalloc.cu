@@ -79,7 +79,7 @@ double * scratch_for_current_device()
 template <typename R>
 __global__ void __launch_bounds__(TOTALS_THREADS) k_totals_part(R const * rec, int rs, int neq,
                                                                 double const * clvol, int64_t ngst, int64_t ncell,
-                                                                double * scratch)
+                                                                R const * comp, double * scratch)
 {
     __shared__ double sh[TOTALS_THREADS / 32];
     double s[5] = {0, 0, 0, 0, 0};
@@ -92,7 +92,12 @@ __global__ void __launch_bounds__(TOTALS_THREADS) k_totals_part(R const * rec, i
         double const v = clvol[row];
         for (int i = 0; i < neq; ++i)
         {
-            double const y = double(rec[row * rs + i]) * v - c[i];
+            double q = double(rec[row * rs + i]);
+            if (comp)
+            {
+                q += double(comp[i * ncell + icl]); // the FP32 state's residual
+            }
+            double const y = q * v - c[i];
             double const t = s[i] + y;
             c[i] = (t - s[i]) - y;
             s[i] = t;
@@ -162,10 +167,12 @@ int scg_euler_totals_noalloc(scg_euler * core, double * out)
         {
             if (v.fp32)
                 k_totals_part<float><<<nblk, TOTALS_THREADS, 0, v.stream>>>(
-                    static_cast<float const *>(v.rec), v.rec_stride, v.neq, v.clvol, v.ngstcell, v.ncell, scratch);
+                    static_cast<float const *>(v.rec), v.rec_stride, v.neq, v.clvol, v.ngstcell, v.ncell,
+                    static_cast<float const *>(v.comp), scratch);
             else
                 k_totals_part<double><<<nblk, TOTALS_THREADS, 0, v.stream>>>(
-                    static_cast<double const *>(v.rec), v.rec_stride, v.neq, v.clvol, v.ngstcell, v.ncell, scratch);
+                    static_cast<double const *>(v.rec), v.rec_stride, v.neq, v.clvol, v.ngstcell, v.ncell,
+                    static_cast<double const *>(v.comp), scratch);
             scg::launched(v.stream, "totals_noalloc_part");
         }
         k_totals_final<<<1, 32, 0, v.stream>>>(nblk, v.neq, scratch);
