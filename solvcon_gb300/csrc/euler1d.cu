@@ -13,7 +13,9 @@
  * only points the half step neither reads nor writes), and update_cfl (which
  * reads only the kernel points) is folded into the same kernel, so a full
  * march_alpha step is two launches.  The fine-grained methods run as separate
- * kernels built from the same device routines.
+ * kernels built from the same device routines.  The FP32 core (Euler1D32,
+ * not in the reference) keeps its state split by parity in a layout of its
+ * own and updates four outputs per thread; see the comment above it.
  */
 
 #include "../../include/scg.h"
@@ -45,7 +47,7 @@ struct Tiny1D<float>
     static constexpr float V = 1.e-30f;
 };
 
-// Coordinates stay FP64 (the grid); the state, gamma and cfl are R.
+// The FP64 core's device state: the reference's [n][3] tables.
 template <typename R>
 struct E1DArgs
 {
@@ -56,11 +58,6 @@ struct E1DArgs
     R * cfl;
     int64_t n;
     double hdt, qdt;
-    // FP32 core: the grid spacing of each point, x - xneg and xpos - x,
-    // formed in FP64 from the coordinates once; and dt/2, dt/4 in R.
-    float const * dxm;
-    float const * dxp;
-    R hdt_r, qdt_r;
 };
 
 // The solution-element kernel at point ic (Euler1DKernel::set_value and
@@ -68,8 +65,6 @@ struct E1DArgs
 // the value up at the point, plus the two half fluxes of calc_flux_ll/lr
 // (Euler1DCore.hpp:246-266).  Reciprocals of rho are formed once: for any
 // density above ~1e-50 the reference's denominators rho^k + tiny equal rho^k.
-// FP64: distances formed from the coordinates.  FP32: distances formed in
-// FP32 from the point's two spacings, each rounded once from FP64.
 template <typename R>
 struct K1D
 {
@@ -78,31 +73,16 @@ struct K1D
     R up[3];
     R ll[3]; // flux through the lower-left of the CE to the right
     R lr[3]; // flux through the lower-right of the CE to the left
-    // FP32 delta form: the state u, up - u, and ll / lr without their
-    // dx * u parts (the caller adds those relative to the output point).
-    R u[3];
-    R upd[3];
-    R llp[3];
-    R lrp[3];
-    R dm, dp; // FP32: x - xneg, xpos - x
 };
 
 template <typename R>
 __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> & k)
 {
     R const ga = a.gamma[ic];
-    double xctr = 0.0;
-    if constexpr (sizeof(R) == 8)
-    {
-        k.x = a.coord[ic];
-        k.xneg = a.coord[ic - 1];
-        k.xpos = a.coord[ic + 1];
-        xctr = (k.xpos + k.xneg) * 0.5;
-    }
-    else
-    {
-        k.x = k.xneg = k.xpos = 0.0; // the FP32 path works from dm, dp
-    }
+    k.x = a.coord[ic];
+    k.xneg = a.coord[ic - 1];
+    k.xpos = a.coord[ic + 1];
+    double const xctr = (k.xpos + k.xneg) * 0.5;
     R u[3], ux[3];
     for (int i = 0; i < 3; ++i)
     {
@@ -135,49 +115,21 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
     {
         ft[i] = jac[i][0] * ut[0] + jac[i][1] * ut[1] + jac[i][2] * ut[2];
     }
-    if constexpr (sizeof(R) == 4)
+    R const hdt = R(a.hdt), qdt = R(a.qdt);
+    R const dxctr = R(k.x - xctr);
+    R const dxl = R(k.xpos - k.x);
+    R const dml = R(0.5 * (k.x + k.xpos) - xctr);
+    R const dxr = R(k.x - k.xneg);
+    R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
+    for (int i = 0; i < 3; ++i)
     {
-        // All in FP32 from the point's spacing: with dm = x - xneg and
-        // dp = xpos - x, x - xctr = (dm - dp) / 2, and the BCE midpoints
-        // sit at dm / 2 and -dp / 2 from the centre.
-        R const hdt = a.hdt_r, qdt = a.qdt_r;
-        R const dm = a.dxm[ic];
-        R const dp = a.dxp[ic];
-        k.dm = dm;
-        k.dp = dp;
-        R const dxctr = R(0.5) * (dm - dp);
-        R const dxl = dp;
-        R const dml = R(0.5) * dm;
-        R const dxr = dm;
-        R const dmr = R(-0.5) * dp;
-        for (int i = 0; i < 3; ++i)
-        {
-            k.u[i] = u[i];
-            k.upd[i] = dxctr * ux[i] + hdt * ut[i];
-            k.up[i] = u[i] + k.upd[i]; // for the so1-only half step
-            R const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
-            k.llp[i] = dxl * dml * ux[i] + hdt * tf;
-            k.lrp[i] = dxr * dmr * ux[i] - hdt * tf;
-        }
+        k.up[i] = u[i] + dxctr * ux[i] + hdt * ut[i];
     }
-    else
+    for (int i = 0; i < 3; ++i)
     {
-        R const hdt = R(a.hdt), qdt = R(a.qdt);
-        R const dxctr = R(k.x - xctr);
-        R const dxl = R(k.xpos - k.x);
-        R const dml = R(0.5 * (k.x + k.xpos) - xctr);
-        R const dxr = R(k.x - k.xneg);
-        R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
-        for (int i = 0; i < 3; ++i)
-        {
-            k.up[i] = u[i] + dxctr * ux[i] + hdt * ut[i];
-        }
-        for (int i = 0; i < 3; ++i)
-        {
-            R const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
-            k.ll[i] = dxl * (u[i] + dml * ux[i]) + hdt * tf;
-            k.lr[i] = dxr * (u[i] + dmr * ux[i]) - hdt * tf;
-        }
+        R const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
+        k.ll[i] = dxl * (u[i] + dml * ux[i]) + hdt * tf;
+        k.lr[i] = dxr * (u[i] + dmr * ux[i]) - hdt * tf;
     }
 }
 
@@ -192,7 +144,6 @@ __device__ __forceinline__ R rho_recip(E1DArgs<R> const & a, int64_t it)
 }
 
 __device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
-__device__ __forceinline__ float sqrt_r(float x) { return sqrtf(x); }
 
 template <typename R>
 __device__ __forceinline__ void cfl_at(E1DArgs<R> const & a, int64_t it, double hdt, R r)
@@ -207,18 +158,9 @@ __device__ __forceinline__ void cfl_at(E1DArgs<R> const & a, int64_t it, double 
     // the square root of a correctly rounded square returns the operand's
     // magnitude (barring overflow or underflow of the square).
     R const wspd = sqrt_r(ga * pr * r) + fabs(m) * r;
-    if constexpr (sizeof(R) == 4)
-    {
-        R const dxpos = a.dxp[it];
-        R const dxneg = a.dxm[it];
-        a.cfl[it] = a.hdt_r * wspd / (dxpos < dxneg ? dxpos : dxneg);
-    }
-    else
-    {
-        double const dxpos = a.coord[it + 1] - a.coord[it];
-        double const dxneg = a.coord[it] - a.coord[it - 1];
-        a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
-    }
+    double const dxpos = a.coord[it + 1] - a.coord[it];
+    double const dxneg = a.coord[it] - a.coord[it - 1];
+    a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
 }
 
 // The W-alpha gradient (march_half_so1_alpha, Euler1DCore.hpp:284-320).
@@ -235,97 +177,6 @@ __device__ __forceinline__ R wgrad(R duxn, R duxp)
     return (fap * duxn + fan * duxp) / (fap + fan + Tiny1D<R>::V);
 }
 
-// The FP32 half step in delta form: each new so0 is the old value at the
-// point plus the change, formed from the kernels' states relative to it
-// (dxl (u_l - u0) + dxr (u_r - u0) + the flux terms, over dxl + dxr), and the
-// gradient's differences likewise, so FP32 rounding scales with the changes
-// and not with the state.  The copy-out boundary treatment as in k_half.
-template <int ALPHA, bool DO_CFL, bool BND>
-__device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t start, int64_t nout)
-{
-    using R = float;
-    __shared__ R s_u[B1D + 1][3];
-    __shared__ R s_upd[B1D + 1][3];
-    __shared__ R s_lrp[B1D + 1][3];
-    __shared__ R s_dm[B1D + 1]; // x - xneg of each kernel
-    int64_t const j0 = static_cast<int64_t>(blockIdx.x) * B1D;
-    int64_t const j = j0 + threadIdx.x;
-    K1D<R> k;
-    bool const have = j <= nout;
-    if (have)
-    {
-        derive(a, start + 2 * j, k);
-        for (int i = 0; i < 3; ++i)
-        {
-            s_u[threadIdx.x][i] = k.u[i];
-            s_upd[threadIdx.x][i] = k.upd[i];
-            s_lrp[threadIdx.x][i] = k.lrp[i];
-        }
-        s_dm[threadIdx.x] = k.dm;
-    }
-    if (threadIdx.x == 0)
-    {
-        int64_t const jh = j0 + B1D; // halo kernel on the right
-        if (jh <= nout)
-        {
-            K1D<R> h;
-            derive(a, start + 2 * jh, h);
-            for (int i = 0; i < 3; ++i)
-            {
-                s_u[B1D][i] = h.u[i];
-                s_upd[B1D][i] = h.upd[i];
-                s_lrp[B1D][i] = h.lrp[i];
-            }
-            s_dm[B1D] = h.dm;
-        }
-    }
-    __syncthreads();
-    if (have && j < nout)
-    {
-        int64_t const ic = start + 2 * j;
-        // The output point ic + 1 between kernels ic (left) and ic + 2.
-        R const dxl = k.dp;
-        R const dxr = s_dm[threadIdx.x + 1];
-        R const idx = R(1) / (dxl + dxr);
-        R d[3];
-        for (int i = 0; i < 3; ++i)
-        {
-            R const u0 = a.so0[(ic + 1) * 3 + i];
-            d[i] = (dxl * (k.u[i] - u0) + dxr * (s_u[threadIdx.x + 1][i] - u0) + k.llp[i] +
-                    s_lrp[threadIdx.x + 1][i]) *
-                   idx;
-            R const v = u0 + d[i];
-            if constexpr (ALPHA > 0)
-            {
-                // The gradient's differences v - up_l and up_r - v, each
-                // from small terms: (u0 - u_l) + d - (up_l - u_l), and
-                // (u_r - u0) + (up_r - u_r) - d.
-                R const idn = R(1) / dxl;
-                R const idp = R(1) / dxr;
-                R const duxn = ((u0 - k.u[i]) + d[i] - k.upd[i]) * idn;
-                R const duxp = ((s_u[threadIdx.x + 1][i] - u0) + s_upd[threadIdx.x + 1][i] - d[i]) * idp;
-                a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
-            }
-            a.so0[(ic + 1) * 3 + i] = v;
-        }
-        if (DO_CFL)
-        {
-            cfl_at(a, ic, a.hdt, k.r);
-        }
-    }
-    if (BND && blockIdx.x == 0 && threadIdx.x == 0)
-    {
-        int64_t const l = 1, r = a.n - 2;
-        for (int i = 0; i < 3; ++i)
-        {
-            a.so0[l * 3 + i] = a.so0[(l + 1) * 3 + i];
-            a.so0[r * 3 + i] = a.so0[(r - 1) * 3 + i];
-            a.so1[l * 3 + i] = a.so1[(l + 1) * 3 + i];
-            a.so1[r * 3 + i] = a.so1[(r - 1) * 3 + i];
-        }
-    }
-}
-
 // Fused half step: so0, cfl and (when ALPHA > 0) so1 at one parity; with
 // BND also the copy-out boundary treatment (Euler1DCore.cpp:132-172).
 // Output j is point start + 2j + 1 for j < nout; kernels are at start + 2j for
@@ -333,11 +184,6 @@ __device__ __forceinline__ void half_delta(E1DArgs<float> const & a, int64_t sta
 template <int ALPHA, bool DO_SO0, bool DO_CFL, bool BND, typename R>
 __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64_t nout)
 {
-    if constexpr (sizeof(R) == 4 && DO_SO0)
-    {
-        half_delta<ALPHA, DO_CFL, BND>(a, start, nout);
-    }
-    else
     {
         __shared__ R s_lr[B1D + 1][3];
         __shared__ R s_up[B1D + 1][3];
@@ -354,7 +200,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                 s_lr[threadIdx.x][i] = k.lr[i];
                 s_up[threadIdx.x][i] = k.up[i];
             }
-            s_idxr[threadIdx.x] = sizeof(R) == 4 ? R(1) / k.dm : R(1.0 / (k.x - k.xneg));
+            s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
         }
         if (threadIdx.x == 0)
         {
@@ -368,7 +214,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                     s_lr[B1D][i] = h.lr[i];
                     s_up[B1D][i] = h.up[i];
                 }
-                s_idxr[B1D] = sizeof(R) == 4 ? R(1) / h.dm : R(1.0 / (h.x - h.xneg));
+                s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
             }
         }
         __syncthreads();
@@ -398,7 +244,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
             }
             if constexpr (ALPHA > 0)
             {
-                R const idn = sizeof(R) == 4 ? R(1) / k.dp : R(1.0 / (k.xpos - k.x));
+                R const idn = R(1.0 / (k.xpos - k.x));
                 R const idp = s_idxr[threadIdx.x + 1];
                 for (int i = 0; i < 3; ++i)
                 {
@@ -448,39 +294,6 @@ __global__ void k_bnd1d(E1DArgs<R> a, int which)
     }
 }
 
-// FP64 host tables to and from the FP32 state, converted on the device; the
-// host side read or written in place when it is a mapped scg_host_alloc
-// block, else through a device staging table.
-__global__ void k_e1d_from_f64(double const * in, float * out, int64_t n)
-{
-    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n)
-    {
-        out[i] = float(in[i]);
-    }
-}
-
-__global__ void k_e1d_to_f64(float const * in, double * out, int64_t n)
-{
-    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n)
-    {
-        out[i] = double(in[i]);
-    }
-}
-
-// The FP32 core's grid spacing, x - xneg and xpos - x, formed in FP64 from the
-// coordinates and rounded once (zero where a neighbour is missing).
-__global__ void k_e1d_spacing(double const * coord, float * dxm, float * dxp, int64_t n)
-{
-    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n)
-    {
-        dxm[i] = i > 0 ? float(coord[i] - coord[i - 1]) : 0.f;
-        dxp[i] = i + 1 < n ? float(coord[i + 1] - coord[i]) : 0.f;
-    }
-}
-
 // What the C ABI calls on a 1D core of either precision.
 struct Euler1DBase
 {
@@ -498,9 +311,8 @@ struct Euler1DBase
     cudaStream_t stream = nullptr;
 };
 
-// R = double: the reference's arithmetic; R = float: FP32 state, cfl and
-// gamma, with the coordinates kept in FP64 and the spacing between them
-// formed in FP64 and rounded once to FP32 tables (dxm, dxp).
+// The FP64 core (R = double): the reference's arithmetic on the reference's
+// [n][3] device tables.  The FP32 core is Euler1D32 below.
 template <typename R>
 class Euler1D : public Euler1DBase
 {
@@ -509,7 +321,7 @@ public:
     {
         n = ncoord;
         time_increment = dt;
-        precision = sizeof(R) == 8 ? SCG_FP64 : SCG_FP32;
+        precision = SCG_FP64;
         if (ncoord % 2 == 0)
         {
             throw std::invalid_argument("ncoord cannot be even");
@@ -524,11 +336,6 @@ public:
             b->alloc(static_cast<size_t>(n));
         so0.alloc(static_cast<size_t>(n * 3));
         so1.alloc(static_cast<size_t>(n * 3));
-        if constexpr (sizeof(R) == 4)
-        {
-            dxm.alloc(static_cast<size_t>(n));
-            dxp.alloc(static_cast<size_t>(n));
-        }
         std::vector<double> g(static_cast<size_t>(n), 1.4);
         std::vector<double> z(static_cast<size_t>(n * 3), 0.0);
         set(4, g.data());
@@ -562,7 +369,6 @@ public:
                             "copy");
         }
         sync();
-        c->spacing();
         return c;
     }
 
@@ -590,30 +396,9 @@ public:
             sync();
             return;
         }
-        if constexpr (sizeof(R) == 8)
-        {
-            scg::cuda_check(cudaMemcpyAsync(host, state(which), sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
-                            "D2H");
-            sync();
-        }
-        else
-        {
-            unsigned const grid = static_cast<unsigned>((cnt + 255) / 256);
-            if (double * const dev = static_cast<double *>(scg::mapped_host(host, sizeof(double) * cnt)))
-            {
-                k_e1d_to_f64<<<grid, 256, 0, stream>>>(state(which), dev, static_cast<int64_t>(cnt));
-                scg::launched(stream, "e1d_to_f64");
-            }
-            else
-            {
-                double * const tmp = staging(cnt);
-                k_e1d_to_f64<<<grid, 256, 0, stream>>>(state(which), tmp, static_cast<int64_t>(cnt));
-                scg::launched(stream, "e1d_to_f64");
-                scg::cuda_check(cudaMemcpyAsync(host, tmp, sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
-                                "D2H");
-            }
-            sync();
-        }
+        scg::cuda_check(cudaMemcpyAsync(host, state(which), sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
+                        "D2H");
+        sync();
     }
     void set(int which, double const * host) override
     {
@@ -621,72 +406,15 @@ public:
         if (which == 0)
         {
             put(coord.ptr, host, cnt);
-            spacing();
             return;
         }
-        if constexpr (sizeof(R) == 8)
-        {
-            put(state(which), host, cnt);
-        }
-        else
-        {
-            unsigned const grid = static_cast<unsigned>((cnt + 255) / 256);
-            if (double const * const dev =
-                    static_cast<double const *>(scg::mapped_host(host, sizeof(double) * cnt)))
-            {
-                k_e1d_from_f64<<<grid, 256, 0, stream>>>(dev, state(which), static_cast<int64_t>(cnt));
-                scg::launched(stream, "e1d_from_f64");
-            }
-            else
-            {
-                double * const tmp = staging(cnt);
-                scg::cuda_check(cudaMemcpyAsync(tmp, host, sizeof(double) * cnt, cudaMemcpyHostToDevice, stream),
-                                "H2D");
-                k_e1d_from_f64<<<grid, 256, 0, stream>>>(tmp, state(which), static_cast<int64_t>(cnt));
-                scg::launched(stream, "e1d_from_f64");
-            }
-            sync();
-        }
-    }
-
-    // The FP32 core's spacing tables from the coordinates, after each write
-    // of them.
-    void spacing()
-    {
-        if constexpr (sizeof(R) == 4)
-        {
-            k_e1d_spacing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(coord.ptr, dxm.ptr, dxp.ptr, n);
-            scg::launched(stream, "e1d_spacing");
-            sync();
-        }
-    }
-
-    // Grow-only device table for FP64 host data on its way to or from the
-    // FP32 state.
-    double * staging(size_t cnt)
-    {
-        if (m_staging.n < cnt)
-        {
-            sync();
-            m_staging.alloc(cnt);
-        }
-        return m_staging.ptr;
+        put(state(which), host, cnt);
     }
 
     E1DArgs<R> args()
     {
-        return E1DArgs<R>{coord.ptr,
-                          gamma.ptr,
-                          so0.ptr,
-                          so1.ptr,
-                          cfl.ptr,
-                          n,
-                          time_increment / 2.0,
-                          time_increment / 4.0,
-                          dxm.ptr,
-                          dxp.ptr,
-                          R(time_increment / 2.0),
-                          R(time_increment / 4.0)};
+        return E1DArgs<R>{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
+                          time_increment / 4.0};
     }
 
     // Loop bounds of a half step (Euler1DCore.cpp:73-74, 99-100).
@@ -844,7 +572,667 @@ private:
 
     scg::DevBuf<double> coord;
     scg::DevBuf<R> cfl, so0, so1, gamma;
-    scg::DevBuf<float> dxm, dxp; // the FP32 core's grid spacing
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_alpha = 0;
+};
+
+// ---------------------------------------------------------------------------
+// The FP32 core (not in the reference): FP32 state, cfl and gamma, the
+// coordinates kept in FP64 and the spacing between them formed in FP64 and
+// rounded once.  It keeps its state in a device layout of its own: every
+// quantity split by the parity of the point into two planes (point i -> plane
+// i & 1, index i >> 1).  A half step reads the kernel planes of one parity
+// and writes the output planes of the other, so every line it fetches is
+// used whole, and one thread updates four consecutive outputs with 16-byte
+// loads and stores (the planes are padded to a multiple of four).  The host
+// sees the reference's [n][3] FP64 tables, converted on the device.
+
+constexpr int B32 = 128;
+enum : int
+{
+    PL_SO0 = 0, // 3 planes: so0 of each variable
+    PL_SO1 = 3, // 3 planes: so1
+    PL_GAMMA = 6,
+    PL_CFL = 7,
+    PL_DXM = 8, // x - xneg
+    PL_DXP = 9, // xpos - x
+    PL_COUNT = 10
+};
+
+struct Planes
+{
+    float * base; // [2][PL_COUNT][P]
+    int64_t P;    // plane stride, a multiple of 4
+    int64_t n;
+    float hdt, qdt;
+    __device__ __forceinline__ float * at(int parity, int q) const
+    {
+        return base + (static_cast<int64_t>(parity) * PL_COUNT + q) * P;
+    }
+};
+
+// The solution-element kernel of one point in FP32 delta form: the state u,
+// up - u, and the two half fluxes without their dx * u parts (the caller adds
+// those relative to the output point); r = 1 / (rho + tiny) for update_cfl.
+struct K32
+{
+    float u[3], upd[3], llp[3], lrp[3];
+    float dm, dp, r, ga;
+};
+
+// Euler1DKernel::set_value and derive (Euler1DCore.hpp:193-244) in FP32 from
+// the point's state, gamma and spacing dm = x - xneg, dp = xpos - x.
+__device__ __forceinline__ void derive32(float const * u, float const * ux, float ga, float dm, float dp, float hdt,
+                                         float qdt, K32 & k)
+{
+    float const r = 1.f / (u[0] + Tiny1D<float>::V);
+    float const r2 = r * r;
+    float const m2r2 = u[1] * u[1] * r2;
+    float jac[3][3];
+    jac[0][0] = 0.f;
+    jac[0][1] = 1.f;
+    jac[0][2] = 0.f;
+    jac[1][0] = (ga - 3.f) / 2.f * m2r2;
+    jac[1][1] = -(ga - 3.f) * u[1] * r;
+    jac[1][2] = ga - 1.f;
+    jac[2][0] = (ga - 1.f) * m2r2 * u[1] * r - ga * u[1] * u[2] * r2;
+    jac[2][1] = ga * u[2] * r - 1.5f * (ga - 1.f) * m2r2;
+    jac[2][2] = ga * u[1] * r;
+    float f[3], ut[3], ft[3];
+    f[0] = u[1];
+    f[1] = (ga - 1.f) * u[2] + (3.f - ga) / 2.f * u[1] * u[1] * r;
+    f[2] = ga * u[1] * u[2] * r - (ga - 1.f) / 2.f * u[1] * m2r2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        ut[i] = -jac[i][0] * ux[0] - jac[i][1] * ux[1] - jac[i][2] * ux[2];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        ft[i] = jac[i][0] * ut[0] + jac[i][1] * ut[1] + jac[i][2] * ut[2];
+    }
+    // x - xctr = (dm - dp) / 2, and the BCE midpoints sit at dm / 2 and
+    // -dp / 2 from the centre.
+    float const dxctr = 0.5f * (dm - dp);
+    float const dml = 0.5f * dm;
+    float const dmr = -0.5f * dp;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        k.u[i] = u[i];
+        k.upd[i] = dxctr * ux[i] + hdt * ut[i];
+        float const tf = f[i] - dxctr * ut[i] + qdt * ft[i];
+        k.llp[i] = dp * dml * ux[i] + hdt * tf;
+        k.lrp[i] = dm * dmr * ux[i] - hdt * tf;
+    }
+    k.dm = dm;
+    k.dp = dp;
+    k.r = r;
+    k.ga = ga;
+}
+
+// update_cfl at a kernel point (Euler1DCore.cpp:70-94) from its derivation.
+__device__ __forceinline__ float cfl32(K32 const & k, float hdt)
+{
+    float const m = k.u[1];
+    float const ke = 0.5f * m * m * k.r;
+    float pr = (k.ga - 1.f) * (k.u[2] - ke);
+    pr = (pr + fabsf(pr)) / 2.f;
+    float const wspd = sqrtf(k.ga * pr * k.r) + fabsf(m) * k.r;
+    return hdt * wspd / (k.dp < k.dm ? k.dp : k.dm);
+}
+
+__device__ __forceinline__ float lane(float4 v, int i)
+{
+    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// One half step of the FP32 core, outputs of parity Q from the kernels of the
+// other parity.  Output o (1 <= o <= nout) sits between its left and right
+// kernels: kernel indices o and o + 1 when the outputs are odd points (the
+// first half step), o - 1 and o when they are even.  Thread t updates outputs
+// 4t .. 4t + 3 from the four kernels at the same indices (16-byte loads) and
+// one more (the next index or the previous one), each derived once per
+// thread.  DO_SO0: the new so0 in delta form (each output's old value plus a
+// change formed from the kernels' states relative to it, so FP32 rounding
+// scales with the change); without it so0 is already new and only so1 is
+// formed.  ALPHA > 0: so1 by the W-alpha gradient.  DO_CFL: update_cfl at
+// each output's left kernel.  BND: the copy-out boundary treatment of points
+// 1 and n - 2, which the half step neither reads nor writes.
+template <int ALPHA, bool DO_SO0, bool DO_CFL, bool BND, int Q>
+__global__ void __launch_bounds__(B32) k_half32(Planes a, int64_t nout)
+{
+    constexpr int P = 1 - Q; // parity of the kernels
+    if (BND && blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        int64_t const hi = (a.n - 3) / 2;
+        for (int v = 0; v < 3; ++v)
+        {
+            a.at(1, PL_SO0 + v)[0] = a.at(0, PL_SO0 + v)[1];
+            a.at(1, PL_SO0 + v)[hi] = a.at(0, PL_SO0 + v)[hi];
+            a.at(1, PL_SO1 + v)[0] = a.at(0, PL_SO1 + v)[1];
+            a.at(1, PL_SO1 + v)[hi] = a.at(0, PL_SO1 + v)[hi];
+        }
+    }
+    int64_t const c = 4 * (static_cast<int64_t>(blockIdx.x) * B32 + threadIdx.x);
+    if (c > nout)
+    {
+        return;
+    }
+    // The five kernels in index order: Q = 1 uses c .. c + 4, Q = 0 uses
+    // c - 1 .. c + 3; the one outside the aligned four is the halo.
+    int64_t const h = Q == 1 ? c + 4 : c - 1;
+    // Index -1 (thread 0 of the second half step) serves only output 0,
+    // which is not written: read kernel 0 in its place.
+    int64_t const hc = h < 0 ? 0 : h;
+    float4 const g4 = *reinterpret_cast<float4 const *>(a.at(P, PL_GAMMA) + c);
+    float4 const m4 = *reinterpret_cast<float4 const *>(a.at(P, PL_DXM) + c);
+    float4 const p4 = *reinterpret_cast<float4 const *>(a.at(P, PL_DXP) + c);
+    float4 u4[3], x4[3];
+    float hu[3], hx[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+    {
+        u4[v] = *reinterpret_cast<float4 const *>(a.at(P, PL_SO0 + v) + c);
+        x4[v] = *reinterpret_cast<float4 const *>(a.at(P, PL_SO1 + v) + c);
+        hu[v] = a.at(P, PL_SO0 + v)[hc];
+        hx[v] = a.at(P, PL_SO1 + v)[hc];
+    }
+    float const hg = a.at(P, PL_GAMMA)[hc];
+    float const hm = a.at(P, PL_DXM)[hc];
+    float const hp = a.at(P, PL_DXP)[hc];
+    // Kernel s (0 .. 4) in index order, derived.
+    auto kernel = [&](int s, K32 & k) {
+        float u[3], x[3], ga, dm, dp;
+        int const l = Q == 1 ? s : s - 1; // lane of the aligned four, or the halo
+        if (l < 0 || l > 3)
+        {
+            for (int v = 0; v < 3; ++v)
+            {
+                u[v] = hu[v];
+                x[v] = hx[v];
+            }
+            ga = hg;
+            dm = hm;
+            dp = hp;
+        }
+        else
+        {
+            for (int v = 0; v < 3; ++v)
+            {
+                u[v] = lane(u4[v], l);
+                x[v] = lane(x4[v], l);
+            }
+            ga = lane(g4, l);
+            dm = lane(m4, l);
+            dp = lane(p4, l);
+        }
+        derive32(u, x, ga, dm, dp, a.hdt, a.qdt, k);
+    };
+    // The outputs' so0: their old values (DO_SO0) or the new ones.
+    float4 o4[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+    {
+        o4[v] = *reinterpret_cast<float4 const *>(a.at(Q, PL_SO0 + v) + c);
+    }
+    float nso0[3][4], nso1[3][4], ncfl[4];
+    K32 L; // the left kernel of output k; R its right one
+    kernel(0, L);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        K32 R;
+        kernel(k + 1, R);
+        float const dxl = L.dp;
+        float const dxr = R.dm;
+        float const idx = 1.f / (dxl + dxr);
+#pragma unroll
+        for (int v = 0; v < 3; ++v)
+        {
+            float const u0 = lane(o4[v], k);
+            float d;
+            if constexpr (DO_SO0)
+            {
+                d = (dxl * (L.u[v] - u0) + dxr * (R.u[v] - u0) + L.llp[v] + R.lrp[v]) * idx;
+                nso0[v][k] = u0 + d;
+            }
+            else
+            {
+                d = 0.f; // u0 is the new value already
+                nso0[v][k] = u0;
+            }
+            if constexpr (ALPHA > 0)
+            {
+                // The gradient's differences v - up_l and up_r - v from small
+                // terms: (u0 - u_l) + d - (up_l - u_l), (u_r - u0) + (up_r - u_r) - d.
+                float const duxn = ((u0 - L.u[v]) + d - L.upd[v]) / dxl;
+                float const duxp = ((R.u[v] - u0) + R.upd[v] - d) / dxr;
+                nso1[v][k] = wgrad<ALPHA>(duxn, duxp);
+            }
+        }
+        if constexpr (DO_CFL)
+        {
+            ncfl[k] = cfl32(L, a.hdt);
+        }
+        L = R;
+    }
+    bool const whole = c >= 1 && c + 3 <= nout;
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+    {
+        float * const s0 = a.at(Q, PL_SO0 + v) + c;
+        float * const s1 = a.at(Q, PL_SO1 + v) + c;
+        if (whole)
+        {
+            if constexpr (DO_SO0)
+            {
+                *reinterpret_cast<float4 *>(s0) = make_float4(nso0[v][0], nso0[v][1], nso0[v][2], nso0[v][3]);
+            }
+            if constexpr (ALPHA > 0)
+            {
+                *reinterpret_cast<float4 *>(s1) = make_float4(nso1[v][0], nso1[v][1], nso1[v][2], nso1[v][3]);
+            }
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                if (c + k >= 1 && c + k <= nout)
+                {
+                    if constexpr (DO_SO0)
+                    {
+                        s0[k] = nso0[v][k];
+                    }
+                    if constexpr (ALPHA > 0)
+                    {
+                        s1[k] = nso1[v][k];
+                    }
+                }
+            }
+        }
+    }
+    if constexpr (DO_CFL)
+    {
+        // The left kernel of output o is kernel o (Q = 1) or o - 1 (Q = 0).
+        float * const cf = a.at(P, PL_CFL) + c - (Q == 1 ? 0 : 1);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            if (c + k >= 1 && c + k <= nout)
+            {
+                cf[k] = ncfl[k];
+            }
+        }
+    }
+}
+
+// update_cfl alone at count kernel points of one parity from index i0.
+__global__ void k_cfl32(Planes a, int parity, int64_t i0, int64_t count)
+{
+    int64_t const j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= count)
+    {
+        return;
+    }
+    int64_t const i = i0 + j;
+    float u[3], x[3];
+    for (int v = 0; v < 3; ++v)
+    {
+        u[v] = a.at(parity, PL_SO0 + v)[i];
+        x[v] = a.at(parity, PL_SO1 + v)[i];
+    }
+    K32 k;
+    derive32(u, x, a.at(parity, PL_GAMMA)[i], a.at(parity, PL_DXM)[i], a.at(parity, PL_DXP)[i], a.hdt, a.qdt, k);
+    a.at(parity, PL_CFL)[i] = cfl32(k, a.hdt);
+}
+
+// treat_boundary_so0 / so1: points 1 and n - 2 from points 2 and n - 3.
+__global__ void k_bnd32(Planes a, int q0)
+{
+    int64_t const hi = (a.n - 3) / 2;
+    for (int v = 0; v < 3; ++v)
+    {
+        a.at(1, q0 + v)[0] = a.at(0, q0 + v)[1];
+        a.at(1, q0 + v)[hi] = a.at(0, q0 + v)[hi];
+    }
+}
+
+// Host table <-> planes.  Table t[i * width + v] of point i (width 3 for so0
+// and so1, 1 for cfl and gamma) goes to plane q0 + v of parity i & 1 at
+// index i >> 1.
+__global__ void k_planes_from_f64(Planes a, int q0, int width, double const * t)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < a.n)
+    {
+        for (int v = 0; v < width; ++v)
+        {
+            a.at(static_cast<int>(i & 1), q0 + v)[i >> 1] = float(t[i * width + v]);
+        }
+    }
+}
+
+__global__ void k_planes_to_f64(Planes a, int q0, int width, double * t)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < a.n)
+    {
+        for (int v = 0; v < width; ++v)
+        {
+            t[i * width + v] = double(a.at(static_cast<int>(i & 1), q0 + v)[i >> 1]);
+        }
+    }
+}
+
+// The spacing planes from the FP64 coordinates, rounded once (zero where a
+// neighbour is missing).
+__global__ void k_planes_spacing(Planes a, double const * coord)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < a.n)
+    {
+        int const p = static_cast<int>(i & 1);
+        a.at(p, PL_DXM)[i >> 1] = i > 0 ? float(coord[i] - coord[i - 1]) : 0.f;
+        a.at(p, PL_DXP)[i >> 1] = i + 1 < a.n ? float(coord[i + 1] - coord[i]) : 0.f;
+    }
+}
+
+class Euler1D32 : public Euler1DBase
+{
+public:
+    Euler1D32(int64_t ncoord, double dt)
+    {
+        n = ncoord;
+        time_increment = dt;
+        precision = SCG_FP32;
+        if (ncoord % 2 == 0)
+        {
+            throw std::invalid_argument("ncoord cannot be even");
+        }
+        if (ncoord < 5)
+        {
+            throw std::invalid_argument("Euler1DCore: ncoord must be at least 5");
+        }
+        scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        coord.alloc(static_cast<size_t>(n));
+        // Each plane holds (n + 1) / 2 points plus room for the last thread's
+        // 16-byte accesses past the end.
+        P = (((n + 1) / 2 + 8) + 3) / 4 * 4;
+        planes.alloc(static_cast<size_t>(2 * PL_COUNT * P));
+        scg::cuda_check(cudaMemsetAsync(planes.ptr, 0, planes.bytes(), stream), "memset");
+        std::vector<double> g(static_cast<size_t>(n), 1.4);
+        set(4, g.data());
+        std::vector<double> z(static_cast<size_t>(n), 0.0);
+        set(0, z.data());
+    }
+
+    ~Euler1D32() override
+    {
+        if (graph_exec)
+            cudaGraphExecDestroy(graph_exec);
+        if (stream)
+        {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    std::unique_ptr<Euler1DBase> clone() override
+    {
+        auto c = std::make_unique<Euler1D32>(n, time_increment);
+        scg::cuda_check(cudaMemcpyAsync(c->coord.ptr, coord.ptr, sizeof(double) * static_cast<size_t>(n),
+                                        cudaMemcpyDeviceToDevice, stream),
+                        "copy");
+        scg::cuda_check(cudaMemcpyAsync(c->planes.ptr, planes.ptr, planes.bytes(), cudaMemcpyDeviceToDevice, stream),
+                        "copy");
+        sync();
+        return c;
+    }
+
+    Planes args() const
+    {
+        return Planes{planes.ptr, P, n, float(time_increment / 2.0), float(time_increment / 4.0)};
+    }
+
+    int64_t count(int which) const override { return (which == 2 || which == 3) ? n * 3 : n; }
+
+    // 1 cfl, 2 so0, 3 so1, 4 gamma -> first plane and width.
+    static void plane_of(int which, int & q0, int & width)
+    {
+        switch (which)
+        {
+        case 1: q0 = PL_CFL; width = 1; break;
+        case 2: q0 = PL_SO0; width = 3; break;
+        case 3: q0 = PL_SO1; width = 3; break;
+        case 4: q0 = PL_GAMMA; width = 1; break;
+        default: throw std::invalid_argument("Euler1DCore: unknown array id " + std::to_string(which));
+        }
+    }
+
+    void get(int which, double * host) override
+    {
+        size_t const cnt = static_cast<size_t>(count(which));
+        if (which == 0)
+        {
+            scg::cuda_check(cudaMemcpyAsync(host, coord.ptr, sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream),
+                            "D2H");
+            sync();
+            return;
+        }
+        int q0, width;
+        plane_of(which, q0, width);
+        unsigned const grid = static_cast<unsigned>((n + 255) / 256);
+        if (double * const dev = static_cast<double *>(scg::mapped_host(host, sizeof(double) * cnt)))
+        {
+            k_planes_to_f64<<<grid, 256, 0, stream>>>(args(), q0, width, dev);
+            scg::launched(stream, "e1d_planes_to_f64");
+        }
+        else
+        {
+            double * const tmp = staging(cnt);
+            k_planes_to_f64<<<grid, 256, 0, stream>>>(args(), q0, width, tmp);
+            scg::launched(stream, "e1d_planes_to_f64");
+            scg::cuda_check(cudaMemcpyAsync(host, tmp, sizeof(double) * cnt, cudaMemcpyDeviceToHost, stream), "D2H");
+        }
+        sync();
+    }
+
+    void set(int which, double const * host) override
+    {
+        size_t const cnt = static_cast<size_t>(count(which));
+        unsigned const grid = static_cast<unsigned>((n + 255) / 256);
+        if (which == 0)
+        {
+            scg::cuda_check(cudaMemcpyAsync(coord.ptr, host, sizeof(double) * cnt, cudaMemcpyHostToDevice, stream),
+                            "H2D");
+            k_planes_spacing<<<grid, 256, 0, stream>>>(args(), coord.ptr);
+            scg::launched(stream, "e1d_planes_spacing");
+            sync();
+            return;
+        }
+        int q0, width;
+        plane_of(which, q0, width);
+        if (double const * const dev = static_cast<double const *>(scg::mapped_host(host, sizeof(double) * cnt)))
+        {
+            k_planes_from_f64<<<grid, 256, 0, stream>>>(args(), q0, width, dev);
+            scg::launched(stream, "e1d_planes_from_f64");
+        }
+        else
+        {
+            double * const tmp = staging(cnt);
+            scg::cuda_check(cudaMemcpyAsync(tmp, host, sizeof(double) * cnt, cudaMemcpyHostToDevice, stream), "H2D");
+            k_planes_from_f64<<<grid, 256, 0, stream>>>(args(), q0, width, tmp);
+            scg::launched(stream, "e1d_planes_from_f64");
+        }
+        sync();
+    }
+
+    // Grow-only device table for FP64 host data on its way to or from the
+    // planes.
+    double * staging(size_t cnt)
+    {
+        if (m_staging.n < cnt)
+        {
+            sync();
+            m_staging.alloc(cnt);
+        }
+        return m_staging.ptr;
+    }
+
+    // Outputs of a half step (Euler1DCore.cpp:97-100): odd = false writes the
+    // odd points 3 .. n - 4, odd = true the even points 2 .. n - 3; either
+    // way indices 1 .. nout of the output planes.
+    int64_t nout_of(bool odd) const { return odd ? (n - 3) / 2 : (n - 5) / 2; }
+
+    template <int ALPHA, bool SO0, bool CFL, bool BND>
+    void half(bool odd)
+    {
+        int64_t const nout = nout_of(odd);
+        if (nout <= 0)
+        {
+            return;
+        }
+        int64_t const threads = nout / 4 + 1;
+        unsigned const grid = static_cast<unsigned>((threads + B32 - 1) / B32);
+        if (odd)
+        {
+            k_half32<ALPHA, SO0, CFL, BND, 0><<<grid, B32, 0, stream>>>(args(), nout);
+        }
+        else
+        {
+            k_half32<ALPHA, SO0, CFL, BND, 1><<<grid, B32, 0, stream>>>(args(), nout);
+        }
+        scg::launched(stream, "e1d_half32");
+    }
+
+    // update_cfl(odd_plane) (Euler1DCore.cpp:70-94): the kernel points of the
+    // half step, the even points 2 .. n - 5 (indices 1 ..) or the odd points
+    // 1 .. n - 4 (indices 0 ..).
+    void cfl_plane(bool odd)
+    {
+        int64_t const count = nout_of(odd);
+        if (count > 0)
+        {
+            k_cfl32<<<static_cast<unsigned>((count + 255) / 256), 256, 0, stream>>>(args(), odd ? 1 : 0, odd ? 0 : 1,
+                                                                                  count);
+            scg::launched(stream, "e1d_cfl32");
+        }
+    }
+
+    void op(int which, int odd, int alpha) override
+    {
+        switch (which)
+        {
+        case 0: // update_cfl
+            cfl_plane(odd != 0);
+            break;
+        case 1: // march_half_so0
+            half<0, true, false, false>(odd != 0);
+            break;
+        case 2: // march_half_so1_alpha
+            if (alpha == 1)
+                half<1, false, false, false>(odd != 0);
+            else
+                half<2, false, false, false>(odd != 0);
+            break;
+        case 3: // treat_boundary_so0
+        case 4: // treat_boundary_so1
+            k_bnd32<<<1, 1, 0, stream>>>(args(), which == 3 ? PL_SO0 : PL_SO1);
+            scg::launched(stream, "e1d_bnd32");
+            break;
+        case 5: // setup_march
+            cfl_plane(false);
+            break;
+        case 6: // march_half1_alpha
+            if (alpha == 1)
+                half<1, true, true, false>(false);
+            else
+                half<2, true, true, false>(false);
+            break;
+        case 7: // march_half2_alpha
+            if (alpha == 1)
+                half<1, true, true, false>(true);
+            else
+                half<2, true, true, false>(true);
+            break;
+        default:
+            throw std::invalid_argument("Euler1DCore: unknown operation " + std::to_string(which));
+        }
+        sync();
+    }
+
+    // One march_alpha step: half 1 with the boundary treatment fused, half 2.
+    void step(int alpha)
+    {
+        if (alpha == 1)
+        {
+            half<1, true, true, true>(false);
+            half<1, true, true, false>(true);
+        }
+        else
+        {
+            half<2, true, true, true>(false);
+            half<2, true, true, false>(true);
+        }
+    }
+
+    void march(int alpha, int64_t steps) override
+    {
+        if (alpha != 1 && alpha != 2)
+        {
+            throw std::invalid_argument("Euler1DCore: alpha must be 1 or 2");
+        }
+        int64_t const chunks = steps / GRAPH_STEPS;
+        if (chunks > 0)
+        {
+            if (!graph_exec || graph_alpha != alpha)
+            {
+                capture(alpha);
+            }
+            for (int64_t c = 0; c < chunks; ++c)
+            {
+                scg::cuda_check(cudaGraphLaunch(graph_exec, stream), "cudaGraphLaunch");
+                scg::g_launches.fetch_add(2 * GRAPH_STEPS, std::memory_order_relaxed);
+            }
+        }
+        for (int64_t s = chunks * GRAPH_STEPS; s < steps; ++s)
+        {
+            step(alpha);
+        }
+    }
+
+    void capture(int alpha)
+    {
+        sync();
+        if (graph_exec)
+        {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        scg::cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "BeginCapture");
+        int64_t const before = scg::g_launches.load();
+        for (int s = 0; s < GRAPH_STEPS; ++s)
+        {
+            step(alpha);
+        }
+        scg::g_launches.store(before); // captured, not launched
+        scg::cuda_check(cudaStreamEndCapture(stream, &g), "EndCapture");
+        scg::cuda_check(cudaGraphInstantiate(&graph_exec, g, 0), "GraphInstantiate");
+        cudaGraphDestroy(g);
+        graph_alpha = alpha;
+    }
+
+    void sync() override { scg::cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+
+private:
+    static constexpr int GRAPH_STEPS = 32;
+    scg::DevBuf<double> coord;
+    scg::DevBuf<float> planes;
+    int64_t P = 0;
     scg::DevBuf<double> m_staging;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
@@ -872,7 +1260,7 @@ int scg_e1d_create_precision(int64_t ncoord, double time_increment, int precisio
         if (precision == SCG_FP64)
             h->c = std::make_unique<Euler1D<double>>(ncoord, time_increment);
         else if (precision == SCG_FP32)
-            h->c = std::make_unique<Euler1D<float>>(ncoord, time_increment);
+            h->c = std::make_unique<Euler1D32>(ncoord, time_increment);
         else
             throw std::invalid_argument("Euler1DCore: precision must be SCG_FP64 or SCG_FP32");
         *out = h.release();
