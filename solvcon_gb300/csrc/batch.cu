@@ -249,7 +249,16 @@ public:
         }
         if (!tl.empty())
         {
-            scg::cuda_check(cudaMemcpy(tiles.ptr, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice), "H2D");
+            // On the batch's own stream, then waited for: a plain cudaMemcpy
+            // from pageable memory returns before its DMA lands and is not
+            // ordered with this non-blocking stream, so the next launch could
+            // read a work list half old, half new (each thread reads its
+            // tile, and the two halves of a block would stage argument words
+            // of two different cores).
+            scg::cuda_check(cudaMemcpyAsync(tiles.ptr, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                            stream),
+                            "H2D");
+            sync();
         }
         size_t const nd = static_cast<size_t>(std::max<int64_t>(ncore, 1));
         for (auto & d : descs)

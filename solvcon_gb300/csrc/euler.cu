@@ -1536,8 +1536,12 @@ public:
 
     void batch_begin() override
     {
+        // The batch kernels run on the batch's stream, which is not ordered
+        // with this core's: whatever this queues here (boundary tables, the
+        // residual's reset, calc_solt) is waited for before returning.
+        bool queued = m_bc_dirty;
         upload_bc();
-        comp_ready();
+        queued = comp_ready() || queued;
         // Exactly what the first substep of march() does before its fused
         // kernel, minus the buffer swap: so0t of the state in rec[cur ^ 1].
         if (!(next_valid && next_buf == (cur ^ 1)) && nrow > 0)
@@ -1546,11 +1550,12 @@ public:
             launched(stream, "calc_solt");
             next_valid = true;
             next_buf = cur ^ 1;
-            sync();
+            queued = true;
         }
-        else if (async_pending || stream != own_stream)
+        // A march of this core, or a caller's stream, may also still run.
+        if (queued || async_pending || stream != own_stream)
         {
-            sync(); // a march of this core, or a caller's stream, may still run
+            sync();
         }
     }
 
@@ -1702,13 +1707,17 @@ private:
         return c;
     }
 
-    void comp_ready()
+    // Starts the residual from zero when it is not live; true when that
+    // queued a memset on the core's stream.
+    bool comp_ready()
     {
         if (sizeof(R) == 4 && !comp_live)
         {
             cuda_check(cudaMemsetAsync(d_comp.ptr, 0, d_comp.bytes(), stream), "memset");
             comp_live = true;
+            return true;
         }
+        return false;
     }
 
     // Host blocks a march also writes so0n / so1n into (deliver()).

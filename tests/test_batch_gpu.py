@@ -159,3 +159,30 @@ def test_retarget_keeps_results_exact():
     other = _cores(2, "fp64", [5])
     assert not b.retarget([other[0][1]])
     assert b.ncore == 3
+
+
+def test_retarget_through_growing_and_shrinking_sets():
+    """Member sets that grow past the work list's capacity (its device table
+    is reallocated and the step graph captured again) and shrink back (the
+    graph's nodes updated in place), each marched right after the retarget:
+    every core still equals its march alone."""
+    from solvcon_gb300.batch import EulerBatch
+    seeds = [3, 11, 17, 29, 31, 37]
+    alone = _cores(2, "fp32", seeds)
+    together = _cores(2, "fp32", seeds)
+    plan = [([0], 2), ([0, 1, 2], 3), ([1, 2, 3, 4, 5], 2), ([2], 4),
+            ([0, 1, 2, 3, 4, 5], 1), ([3, 4], 3), ([5, 0, 1, 2, 3, 4], 2)]
+    b = None
+    for members, steps in plan:
+        for k in members:
+            alone[k][1].march(steps)
+        cores = [together[k][1] for k in members]
+        if b is None:
+            b = EulerBatch(cores, block=64)
+        else:
+            assert b.retarget(cores)
+        assert b.ncore == len(members)
+        b.march(steps)
+    for (_, a), (_, t) in zip(alone, together):
+        np.testing.assert_array_equal(t.so0n.ndarray, a.so0n.ndarray)
+        np.testing.assert_array_equal(t.so1n.ndarray, a.so1n.ndarray)

@@ -78,6 +78,35 @@ def test_budget_limits_resident_set():
         np.testing.assert_array_equal(r.result, ref, "request %d" % r.rid)
 
 
+def test_results_same_alone_in_a_long_mixed_run():
+    """The served workload's mix at a reduced scale: ticks of up to 32 steps
+    (the 1D tubes then replay their captured 32-step graphs while the 2D
+    batch runs), one batch re-pointed at member sets that grow and shrink
+    from tick to tick, and the 1k-100k point tubes.  Every request must
+    still equal its march alone bit for bit."""
+    from solvcon_gb300 import meshgen
+    from solvcon_gb300.serving import Server, alone, make_requests
+    srv = Server(hbm_budget=1 << 34, max_chunk=32, precision="fp32")
+    for key, (n, g, seed) in enumerate([(6, 1.4, 1), (13, 1.2, 2),
+                                        (21, 1.6, 3), (34, 1.3, 4),
+                                        (9, 1.5, 5), (27, 1.1, 6)]):
+        x, t, c = meshgen.tri_square(n, 0.2, seed)
+        mesh = meshgen.build_mesh(2, x, t, c)
+        clcnd = np.asarray(mesh.clcnd.ndarray)[mesh.ngstcell:]
+        state = meshgen.quadrant_state(clcnd, seed, g)
+        faces = np.asarray(mesh.bndfcs.ndarray[:, 0]).copy()
+        srv.add_mesh(key, mesh, state, faces, g, 2e-4 * (1 + key))
+    reqs = make_requests(32, 2000.0, list(range(6)), seed=11,
+                         steps=(33, 140))
+    done = srv.run(reqs)
+    assert sorted(r.rid for r in done) == list(range(len(reqs)))
+    assert srv.rebuilds > 4 and srv.peak_resident >= 4
+    assert any(r.kind == "1d" and r.steps >= 32 for r in done)
+    for r in done:
+        ref, _ = alone(srv, r, "fp32")
+        np.testing.assert_array_equal(r.result, ref, "request %d" % r.rid)
+
+
 def test_oversized_request_is_rejected():
     from solvcon_gb300.serving import Request
     srv = _server(budget=100000)
