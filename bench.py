@@ -63,8 +63,10 @@ ALG_BYTES.update({(w, "fp32-geom64"): ALG_BYTES[(w, "fp32")]
 # (192 B instead of 128 B), which trades DRAM bytes, idle in the FP64-bound
 # march, for FP64 operations.
 NCU_TRAFFIC_PER_CELL = {("tri2d", "fp64"): 769.5,
+                        ("tri2d", "fp32"): 546.6,
                         ("tri2d", "fp32-geom32"): 270.2,
                         ("tet3d", "fp64"): 1337.3,
+                        ("tet3d", "fp32"): 1199.1,
                         ("tet3d", "fp32-geom32"): 627.1}
 NCU_DP_FLOPS_PER_CELL = {("tri2d", "fp64"): 1159.6, ("tet3d", "fp64"): 2717.4}
 
@@ -693,29 +695,34 @@ def dt_for_cfl_g(mesh, state, cfl, gamma):
     return cfl / cmax
 
 
-def run_batch(args, world, rank, dist):
-    """The batched workload: one FP32 batched march of many meshes
-    (autotuned tile, grid policy and cell ordering, CUDA graph per step)
-    against the same meshes marched one after the other in plain FP64."""
+def measure_batch(nmesh, seed, prec, steps, warmup, dist=None, world=1,
+                  tune=True, accuracy=True, local=0):
+    """One FP32 batched march of nmesh meshes of the batched distribution
+    (tile, grid policy and cell ordering autotuned, or Morton order with
+    one block of 128 per tile), CUDA graph per step, against the same
+    meshes marched one after the other in plain FP64.  Returns the figures
+    of the batched workload's line."""
     from solvcon_gb300._lib import launch_count
     from solvcon_gb300.batch import EulerBatch, autotune
-    nmesh = args.nmesh
-    seed = 2026 + 1000 * rank
-    prec = args.precision or "fp32"
 
-    # Autotune tile, grid policy and cell ordering on scratch cores of a
-    # subset of the meshes, each built in both cell orders.
     t_tune = time.perf_counter()
-    sub = list(range(0, nmesh, max(1, nmesh // 32)))
-    cand = {}
-    for order in ("native", "morton"):
-        cand[order] = [setup_core_g(m, s, f, dt_for_cfl_g(m, s, 0.8, g),
-                                    prec, g)
-                       for m, s, f, g in batch_meshes(nmesh, seed,
-                                                      order=order, only=sub)]
-    best, table = autotune(cand["native"], steps=2, repeat=2,
-                           orderings={"morton": cand["morton"]})
-    del cand
+    if tune:
+        # Autotune tile, grid policy and cell ordering on scratch cores of
+        # a subset of the meshes, each built in both cell orders.
+        sub = list(range(0, nmesh, max(1, nmesh // 32)))
+        cand = {}
+        for order in ("native", "morton"):
+            cand[order] = [setup_core_g(m, s, f, dt_for_cfl_g(m, s, 0.8, g),
+                                        prec, g)
+                           for m, s, f, g in batch_meshes(nmesh, seed,
+                                                          order=order,
+                                                          only=sub)]
+        best, table = autotune(cand["native"], steps=2, repeat=2,
+                               orderings={"morton": cand["morton"]})
+        del cand
+    else:
+        best = {"ordering": "morton", "block": 128, "persistent": False}
+        table = None
     t_tune = time.perf_counter() - t_tune
 
     t_setup = time.perf_counter()
@@ -729,108 +736,124 @@ def run_batch(args, world, rank, dist):
     ncell = sum(c.ncell for c in fast)
     batch = EulerBatch(fast, block=best["block"],
                        persistent=best["persistent"])
-    batch.march(args.warmup)
+    batch.march(warmup)
     barrier(dist)
     n0 = launch_count()
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
-        batch.march(args.steps)
+    with ClockSampler(local) as clocks:
+        batch.march(steps)
         ms = batch.last_ms
     launches = launch_count() - n0
     barrier(dist)
     ms_max = reduce_max(dist, ms)
-    value = world * ncell * args.steps / (ms_max * 1e-3)
+    value = world * ncell * steps / (ms_max * 1e-3)
 
     # Plain FP64, one mesh after the other, same steps.
     for c in plain:
-        c.march(args.warmup)
+        c.march(warmup)
     for c in plain:
         c.sync()
     t0 = time.perf_counter()
     for c in plain:
-        c.march_async(args.steps)
+        c.march_async(steps)
     for c in plain:
         c.sync()
     seq_ms = (time.perf_counter() - t0) * 1e3
-    seq_value = ncell * args.steps / (seq_ms * 1e-3)
+    seq_value = ncell * steps / (seq_ms * 1e-3)
 
-    # Accuracy of the FP32 batch against the FP64 marches (same step count),
-    # beside the problem's own sensitivity: the FP64 marches restarted from
-    # states perturbed by 1e-15 relative.
-    rng = np.random.default_rng(7)
-    pert = [setup_core_g(m, s * (1 + 1e-15 * rng.uniform(-1, 1, s.shape)), f,
-                         dt, "fp64", g)
-            for (m, s, f, g), dt in zip(data, dts)]
-    for c in pert:
-        c.march(args.warmup + args.steps)
-    ref = [_body(c) for c in plain]
-    vols = [np.array(m.clvol.ndarray)[m.ngstcell:] for m, *_ in data]
+    acc = None
+    if accuracy:
+        # Accuracy of the FP32 batch against the FP64 marches (same step
+        # count), beside the problem's own sensitivity: the FP64 marches
+        # restarted from states perturbed by 1e-15 relative.
+        rng = np.random.default_rng(7)
+        pert = [setup_core_g(m, s * (1 + 1e-15 * rng.uniform(-1, 1, s.shape)),
+                             f, dt, "fp64", g)
+                for (m, s, f, g), dt in zip(data, dts)]
+        for c in pert:
+            c.march(warmup + steps)
+        ref = [_body(c) for c in plain]
+        vols = [np.array(m.clvol.ndarray)[m.ngstcell:] for m, *_ in data]
 
-    def rel_l1(cores):
-        num, den, worst = np.zeros(4), np.zeros(4), np.zeros(4)
-        for c, r, v in zip(cores, ref, vols):
-            d = (np.abs(_body(c) - r) * v[:, None]).sum(0)
-            a = (np.abs(r) * v[:, None]).sum(0)
-            num += d
-            den += a
-            worst = np.maximum(worst, d / a)
-        return {"rel_l1_aggregate": [float(x) for x in num / den],
-                "rel_l1_worst_mesh": [float(x) for x in worst]}
-    accuracy = {"steps": args.warmup + args.steps,
-                "fp32_vs_fp64": rel_l1(fast),
-                "floor_fp64_perturbed_1e-15_vs_fp64": rel_l1(pert)}
-    del pert
+        def rel_l1(cores):
+            num, den, worst = np.zeros(4), np.zeros(4), np.zeros(4)
+            for c, r, v in zip(cores, ref, vols):
+                d = (np.abs(_body(c) - r) * v[:, None]).sum(0)
+                a = (np.abs(r) * v[:, None]).sum(0)
+                num += d
+                den += a
+                worst = np.maximum(worst, d / a)
+            return {"rel_l1_aggregate": [float(x) for x in num / den],
+                    "rel_l1_worst_mesh": [float(x) for x in worst]}
+        acc = {"steps": warmup + steps, "fp32_vs_fp64": rel_l1(fast),
+               "floor_fp64_perturbed_1e-15_vs_fp64": rel_l1(pert)}
+        del pert
 
     hbm_peak, peak_kind = peaks()
-    per_launch_ms = ms / (2 * args.steps)
+    per_launch_ms = ms / (2 * steps)
     alg = ALG_BYTES[("tri2d", prec)] * ncell
     achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    return {
+        "value": value, "ms_per_step": ms_max / steps, "ncell": ncell,
+        "best": best, "table": table, "t_tune": t_tune, "t_setup": t_setup,
+        "seq_value": seq_value, "accuracy": acc, "launches": launches,
+        "clocks": clocks.summary(),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": None, "kernel": "k_fused_batch",
+                     "alg_bytes_per_cell_substep": ALG_BYTES[("tri2d", prec)],
+                     "launch_ms": per_launch_ms,
+                     "peak_source": peak_kind},
+    }
+
+
+def run_batch(args, world, rank, dist):
+    """The batched workload: one FP32 batched march of many meshes
+    (autotuned tile, grid policy and cell ordering, CUDA graph per step)
+    against the same meshes marched one after the other in plain FP64."""
+    nmesh = args.nmesh
+    prec = args.precision or "fp32"
+    r = measure_batch(nmesh, 2026 + 1000 * rank, prec, args.steps,
+                      args.warmup, dist, world,
+                      local=int(os.environ.get("LOCAL_RANK", "0")))
     line = {
-        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
+        "metric": "cell-steps/s", "value": r["value"], "unit": "cell-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
         "config": {"workload": "batch%d (%d 2D jittered-triangle meshes, "
                                "cells log-uniform in [2k, 200k], per-mesh "
                                "quadrant states, gamma in [1.1, 1.67], CFL "
                                "0.8, slip walls)" % (nmesh, nmesh),
-                   "cells": ncell, "meshes": nmesh, "precision": prec,
-                   "autotune": best, "autotune_table": table,
-                   "autotune_s": t_tune,
+                   "cells": r["ncell"], "meshes": nmesh, "precision": prec,
+                   "autotune": r["best"], "autotune_table": r["table"],
+                   "autotune_s": r["t_tune"],
                    "l2": "state larger than L2 (no flush needed)",
-                   "setup_s": t_setup},
+                   "setup_s": r["t_setup"]},
         "baseline_plain_fp64_sequential": {
-            "value": seq_value, "unit": "cell-steps/s",
-            "speedup_of_batch": value / seq_value},
-        "accuracy_vs_fp64": accuracy,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "traffic": None, "kernel": "k_fused_batch",
-                     "launch_ms": per_launch_ms,
-                     "peak_source": peak_kind},
-        "gpu_launches": launches, "clocks": clocks.summary(),
+            "value": r["seq_value"], "unit": "cell-steps/s",
+            "speedup_of_batch": r["value"] / r["seq_value"]},
+        "accuracy_vs_fp64": r["accuracy"],
+        "roofline": r["roofline"],
+        "gpu_launches": r["launches"], "clocks": r["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def run_serve(args, world, rank, dist):
-    """The served workload: Poisson arrivals of mixed 1D tubes (30%) and 2D
-    meshes (70%, the batched workload's distribution), 200-2000 steps each,
-    served with continuous batching under a 120 GB HBM budget; p50/p99
-    latency and aggregate cell-steps/s per arrival rate, against each
-    request marched alone with the plain FP64 march."""
+def measure_serve(nmesh, nreq, rates, max_chunk, precision, seed=4242):
+    """The served workload at the given Poisson arrival rates (one warm-up
+    pass first, which creates every slot and captures the graphs), and the
+    same requests each marched alone with the plain FP64 march.  Returns
+    (stats per rate, alone-FP64 cell-steps/s, alone seconds)."""
     from solvcon_gb300 import serving
-    nreq = args.nreq
-    data = batch_meshes(args.nmesh, seed=4242 + 1000 * rank)
-    srv = serving.Server(hbm_budget=120 * 2 ** 30, max_chunk=args.max_chunk,
-                         precision=args.precision or "fp32")
+    data = batch_meshes(nmesh, seed=seed)
+    srv = serving.Server(hbm_budget=120 * 2 ** 30, max_chunk=max_chunk,
+                         precision=precision)
     for k, (m, s, f, g) in enumerate(data):
         srv.add_mesh(k, m, s, f, g, dt_for_cfl_g(m, s, 0.8, g))
     keys = list(range(len(data)))
-    # Warm-up pass: creates every slot and captures the graphs.
     srv.run(serving.make_requests(nreq, 1e6, keys, seed=7))
-    rates = [float(r) for r in args.rates.split(",")]
     per_rate = []
     for rate in rates:
         reqs = serving.make_requests(nreq, rate, keys, seed=7)
@@ -855,7 +878,20 @@ def run_serve(args, world, rank, dist):
         cells = srv.meshes[r.mesh_key].mesh.ncell if r.kind == "2d" \
             else r.ncoord
         work += cells * r.steps
-    alone_rate = work / alone_s
+    return per_rate, work / alone_s, alone_s
+
+
+def run_serve(args, world, rank, dist):
+    """The served workload: Poisson arrivals of mixed 1D tubes (30%) and 2D
+    meshes (70%, the batched workload's distribution), 200-2000 steps each,
+    served with continuous batching under a 120 GB HBM budget; p50/p99
+    latency and aggregate cell-steps/s per arrival rate, against each
+    request marched alone with the plain FP64 march."""
+    nreq = args.nreq
+    rates = [float(r) for r in args.rates.split(",")]
+    per_rate, alone_rate, alone_s = measure_serve(
+        args.nmesh, nreq, rates, args.max_chunk, args.precision or "fp32",
+        seed=4242 + 1000 * rank)
     best = max(per_rate, key=lambda s: s["cell_steps_per_s"])
     line = {
         "metric": "cell-steps/s", "value": best["cell_steps_per_s"],
@@ -1166,6 +1202,60 @@ def _desc(w):
             (w["nside"], 6 * w["nside"] ** 3, w["jitter"], w["cfl"]))
 
 
+def headline_figures(local):
+    """The batched and served forms of the march, measured compactly beside
+    the default line so that its record carries them: 512 meshes of the
+    batched distribution in one FP32 batched march (Morton cell order, one
+    block of 128 per tile, no autotuning or accuracy pass) against the same
+    meshes in sequential plain FP64; and the served mix at 2000 req/s (64
+    requests after a warm-up pass) against each request alone in plain
+    FP64.  A failure is recorded in place of the figures."""
+    out = {}
+    try:
+        steps, warmup = 20, 3
+        r = measure_batch(512, 2026, "fp32", steps, warmup, tune=False,
+                          accuracy=False, local=local)
+        out["batched"] = {
+            "metric": "cell-steps/s", "value": r["value"],
+            "unit": "cell-steps/s",
+            "workload": "batch512 (512 2D jittered-triangle meshes, cells "
+                        "log-uniform in [2k, 200k], per-mesh quadrant "
+                        "states, gamma in [1.1, 1.67], CFL 0.8, slip walls)",
+            "cells": r["ncell"],
+            "precision": "fp32 (FP32 state and flux, FP64 geometry)",
+            "steps": steps, "warmup": warmup,
+            "ms_per_step": r["ms_per_step"], "tiles": r["best"],
+            "plain_fp64_sequential": r["seq_value"],
+            "speedup_vs_plain_fp64_sequential": r["value"] / r["seq_value"],
+            "roofline": r["roofline"], "gpu_launches": r["launches"],
+            "clocks": r["clocks"], "setup_s": r["t_setup"]}
+    except Exception as e:  # recorded, the default line still prints
+        out["batched"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    try:
+        nreq, rate = 64, 2000.0
+        per_rate, alone_rate, alone_s = measure_serve(64, nreq, [rate], 32,
+                                                      "fp32")
+        st = per_rate[0]
+        out["served"] = {
+            "metric": "cell-steps/s", "value": st["cell_steps_per_s"],
+            "unit": "cell-steps/s",
+            "workload": "serve (%d requests at %g req/s: 30%% 1D Sod-type "
+                        "tubes of 1k-100k points, 70%% 2D meshes of the "
+                        "batched distribution, 200-2000 steps; HBM budget "
+                        "120 GB; continuous batching, ticks of at most 32 "
+                        "steps)" % (nreq, rate),
+            "precision": "fp32 (FP32 state and flux, FP64 geometry; FP32 "
+                         "tubes)",
+            "p50_latency_s": st["p50_latency_s"],
+            "p99_latency_s": st["p99_latency_s"],
+            "makespan_s": st["makespan_s"],
+            "alone_plain_fp64": alone_rate, "alone_seconds": alone_s,
+            "speedup_vs_alone_plain_fp64": st["cell_steps_per_s"] / alone_rate}
+    except Exception as e:
+        out["served"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1185,6 +1275,8 @@ def main():
     ap.add_argument("--cpu-nside", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="default line: skip the batched and served figures")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cases", default=None,
                     help="accuracy workload: comma-separated subset of "
@@ -1291,6 +1383,12 @@ def main():
                          "nside=%d) for %d steps; %.1f s" % (
                              nproc, ncpu, nside, args.cpu_steps, secs)}
 
+    headline = {}
+    if (rank == 0 and world == 1 and args.workload == "tri2d"
+            and not args.no_headline):
+        del core
+        headline = headline_figures(local)
+
     line = {
         "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -1310,6 +1408,7 @@ def main():
         "gpu_launches": launches, "clocks": clocks.summary(),
         "check": {"finite": finite, "cflo_range": [lo, hi]},
     }
+    line.update(headline)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
