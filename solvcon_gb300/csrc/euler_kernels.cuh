@@ -117,10 +117,54 @@ __device__ __forceinline__ void store_rec(R * base, R const * so0, R const * so0
     }
 }
 
+// A geometry table value, loaded once per cell-substep and streamed: the
+// FP32 3D march (FP64 tables, 816 B per tetrahedron) loads it evict-first,
+// which leaves the caches to the neighbour records (measured on 24.6M
+// tetrahedra: 7.08 -> 6.84 ms per launch; in 2D, and with L1 no-allocate
+// loads, it was slower, so the other marches load it plainly).
+template <int ND, typename R, typename G>
+__device__ __forceinline__ G geo_ld(G const * p)
+{
+    if constexpr (ND == 3 && sizeof(R) == 4 && sizeof(G) == 8)
+    {
+        return __ldcs(p);
+    }
+    else
+    {
+        return ldg(p);
+    }
+}
+
 template <int ND, typename R, typename G>
 __device__ __forceinline__ R fg(MarchArgs<R, G> const & a, int f, int k, int64_t icl)
 {
-    return geo_r<R>(ldg(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
+    return geo_r<R>(geo_ld<ND, R>(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
+}
+
+// The same rounding (IEEE round-to-nearest-even: the same bits over FP32's
+// normal range, where geometry values lie) for the
+// few values the FP32 3D march uses last (the gradient-element displacement
+// P and the two per-cell scalars): there the conversion instruction, on the
+// otherwise idle FP64 pipe, relieves the integer pipe of 14 roundings per
+// tetrahedron (6.84 -> 6.70 ms per 24.6M-cell launch; in 2D it was 1% slower,
+// so 2D rounds everything with integers).
+template <int ND, typename R, typename G>
+__device__ __forceinline__ R geo_late(G v)
+{
+    if constexpr (ND == 3 && sizeof(R) == 4 && sizeof(G) == 8)
+    {
+        return R(v);
+    }
+    else
+    {
+        return geo_r<R>(v);
+    }
+}
+
+template <int ND, typename R, typename G>
+__device__ __forceinline__ R fg_late(MarchArgs<R, G> const & a, int f, int k, int64_t icl)
+{
+    return geo_late<ND, R>(geo_ld<ND, R>(a.fgeo + (static_cast<int64_t>(f) * Geo<ND, G>::KF + k) * a.ncell + icl));
 }
 
 // What calc_soln hands to calc_dsoln of the same cell when the neighbour
@@ -346,7 +390,7 @@ __device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl
             acc[i].add(-fl[i]);
         }
     }
-    R const ivol = geo_r<R>(ldg(a.cgeo + 0 * a.ncell + icl));
+    R const ivol = geo_late<ND, R>(geo_ld<ND, R>(a.cgeo + 0 * a.ncell + icl));
 #pragma unroll
     for (int i = 0; i < NEQ; ++i)
     {
@@ -388,7 +432,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     R const pr = ga1 * (so0n[NEQ - 1] - ke);
     R const pra = (pr + fabs(pr)) / R(2);
     R const wspd = sqr_t(ga * pra * ri) + sqr_t(momsq) * ri;
-    R const cflo = wspd * geo_r<R>(ldg(a.cgeo + 1 * a.ncell + icl));
+    R const cflo = wspd * geo_late<ND, R>(geo_ld<ND, R>(a.cgeo + 1 * a.ncell + icl));
     // pra / (pra + TINY) is exactly 1 whenever TINY does not change pra (any
     // pressure above ~1e-44 in FP64), so the division is taken only below.
     R const prt = pra + Tiny<R>::CFL;
@@ -460,7 +504,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             }
             else
             {
-                idis[f][d] = fg<ND>(a, f, D::K_P + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl);
+                idis[f][d] = fg_late<ND>(a, f, D::K_P + d, icl) + tau * fg<ND>(a, f, D::K_Q + d, icl);
             }
         }
     }
