@@ -52,7 +52,8 @@ __device__ __forceinline__ void fused_batch_tiles(MarchArgs<R, G> const * descs,
             words[threadIdx.x] = reinterpret_cast<int const *>(descs + tl.x)[threadIdx.x];
         }
         __syncthreads();
-        scg::dev::fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(tl.y) + threadIdx.x);
+        scg::dev::fused_thread<ND, R, G, CT1, scg::dev::carry_shared<ND>() ? B : 0>(
+            a, static_cast<int64_t>(tl.y) + threadIdx.x);
     }
 }
 

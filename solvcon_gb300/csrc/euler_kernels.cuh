@@ -10,6 +10,8 @@
 
 #include "euler_device.cuh"
 
+#include <type_traits>
+
 namespace scg
 {
 namespace dev
@@ -234,6 +236,40 @@ struct Carry
     R q[NFC][ND + 2];
 };
 
+// The same sums kept in shared memory instead of registers: one slot per
+// thread and component, component-major (SB threads apart), so a warp's
+// accesses fall in distinct banks; each thread reads only its own slots, so
+// no barrier is needed.  Used for tetrahedra (40 floats per cell), where it
+// frees registers at the same budget: 24.6M tetrahedra 6.70 -> 6.44 ms per
+// launch at 128 registers (at 96 registers it spills and loses); for
+// triangles (24 floats) it was slower at every budget (2D, 2M cells: 0.2356
+// ms in registers, 0.2451 / 0.2505 / 0.2734 ms at 96 / 80 / 72 registers).
+// The single-mesh and batched kernels carry the same way, so a batched core
+// gives the same bits as its own march.
+template <int ND>
+__host__ __device__ constexpr bool carry_shared()
+{
+    return ND == 3;
+}
+template <int ND, int NFC, typename R, int SB>
+struct CarrySh
+{
+    struct Row
+    {
+        R * b;
+        __device__ __forceinline__ R & operator[](int i) const { return b[i * SB]; }
+    };
+    struct Tab
+    {
+        R * b;
+        __device__ __forceinline__ Row operator[](int f) const { return Row{b + f * (ND + 2) * SB}; }
+    };
+    R mm[ND];
+    R mb[ND];
+    Tab p;
+    Tab q;
+};
+
 // Face means of mid and dB (FP32 geometry; zero with FP64 geometry).
 template <int CT, typename R, typename G>
 __device__ __forceinline__ void face_means(MarchArgs<R, G> const & a, int64_t icl, R * mm, R * mb)
@@ -279,9 +315,9 @@ __device__ __forceinline__ void face_means(MarchArgs<R, G> const & a, int64_t ic
 // differences from u0 and d0 receives so0n - u0: in FP32 the absolute
 // rounding then scales with the change, not with the state (the gradients
 // calc_dsoln forms from these differences are O(h) of the state).
-template <int CT, typename R, typename G, bool CACHE = false>
-__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n,
-                                          Carry<CellT<CT>::ND, CellT<CT>::NFC, R> * carry = nullptr,
+template <int CT, typename R, typename G, bool CACHE = false,
+          typename CA = Carry<CellT<CT>::ND, CellT<CT>::NFC, R>>
+__device__ __forceinline__ void soln_cell(MarchArgs<R, G> const & a, int64_t icl, R * so0n, CA * carry = nullptr,
                                           R const * u0 = nullptr, R * d0 = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
@@ -455,10 +491,9 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
 // gathered a second time (calc_soln just read them, so the loads hit in
 // cache); carrying calc_soln's neighbour terms over instead costs more FP64
 // operations, but pays in FP32 for simplices (carry != nullptr, see Carry).
-template <int CT, typename R, typename G>
+template <int CT, typename R, typename G, typename CA = Carry<CellT<CT>::ND, CellT<CT>::NFC, R>>
 __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t icl, R const * so0n, R cflc,
-                                           R * so1n,
-                                           Carry<CellT<CT>::ND, CellT<CT>::NFC, R> const * carry = nullptr,
+                                           R * so1n, CA const * carry = nullptr,
                                            R const * u0 = nullptr, R const * d0 = nullptr)
 {
     constexpr int ND = CellT<CT>::ND;
@@ -991,7 +1026,7 @@ __device__ __forceinline__ void deliver_row(MarchArgs<R, G> const & a, int64_t r
 // substep for its own row and its ghost rows.  Reads only the current records
 // (neighbours' old values) and writes only rows it owns, so one launch covers
 // the whole substep with no grid-wide synchronisation.
-template <int CT, typename R, typename G>
+template <int CT, typename R, typename G, int SB = 0>
 __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t icl)
 {
     constexpr int ND = CellT<CT>::ND;
@@ -1005,7 +1040,15 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
     // kernel, so a core's cells give the same bits in every kernel that
     // marches them (single-type or mixed, alone or batched).
     constexpr bool CARRY = carries<R, CT>();
-    Carry<ND, NFC, R> carry;
+    // SB > 0: the carried sums in shared memory, SB threads per block.
+    using CA = std::conditional_t<(SB > 0 && CARRY), CarrySh<ND, NFC, R, SB>, Carry<ND, NFC, R>>;
+    CA carry;
+    if constexpr (SB > 0 && CARRY)
+    {
+        __shared__ R s_carry[2 * NFC * NEQ * SB];
+        carry.p.b = s_carry + threadIdx.x;
+        carry.q.b = s_carry + NFC * NEQ * SB + threadIdx.x;
+    }
     if constexpr (CARRY)
     {
         face_means<CT, R, G>(a, icl, carry.mm, carry.mb);
@@ -1119,7 +1162,7 @@ __device__ __forceinline__ void fused_cell(MarchArgs<R, G> const & a, int64_t ic
 // t - ncell after that.  CT1 = 0 dispatches on each cell's type; a nonzero
 // CT1 compiles the one cell type of a single-type mesh, whose kernel then
 // needs only that type's registers.
-template <int ND, typename R, typename G, int CT1 = 0>
+template <int ND, typename R, typename G, int CT1 = 0, int SB = 0>
 __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t t)
 {
     if (t < a.ncell)
@@ -1128,7 +1171,7 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
         if constexpr (CT1 != 0)
         {
             (void)ct;
-            fused_cell<CT1, R, G>(a, t);
+            fused_cell<CT1, R, G, SB>(a, t);
         }
         else if constexpr (ND == 2)
         {
@@ -1170,7 +1213,8 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
 template <int ND, typename R, typename G, int CT1 = 0>
 __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
 {
-    fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(
+        a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
 // The same kernel asking the compiler for MINB resident blocks of 128
@@ -1180,7 +1224,8 @@ __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
 template <int ND, typename R, typename G, int CT1, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_fused_mb(MarchArgs<R, G> a)
 {
-    fused_thread<ND, R, G, CT1>(a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(
+        a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
 }
 
 } // namespace dev
