@@ -227,12 +227,13 @@ def time_resident(core, steps):
 def time_e2e(core, steps):
     """K steps through the C ABI with host state: per step the state (so0n,
     so1n) is copied from pinned host memory, one march step runs, and the new
-    state comes back into the same pinned buffers.  The buffers are
-    registered once with scg_euler_deliver: an FP64 march's last substep
-    writes the new state over the host link as it computes it, an FP32
-    march queues a coalesced gather into them after it; the step ends when
-    scg_euler_sync returns with the state in host memory.  Wall time around
-    the whole loop."""
+    state comes back into the same pinned buffers.  scg_euler_march_from_host
+    takes the state from the buffers while the step's first substep marches
+    the cells whose rows are already up; the buffers are registered once with
+    scg_euler_deliver: an FP64 march's last substep writes the new state over
+    the host link as it computes it, an FP32 march queues a coalesced gather
+    into them after it; the step ends when scg_euler_sync returns with the
+    state in host memory.  Wall time around the whole loop."""
     from solvcon_gb300._lib import check, lib
     ids = {"so0n": 5, "so1n": 8}
     bufs = {}
@@ -251,12 +252,10 @@ def time_e2e(core, steps):
         p, view = bufs[name]
         check(lib.scg_euler_deliver(h, ids[name], p, view.size))
     core.sync()
+    (p0, v0), (p1, v1) = bufs["so0n"], bufs["so1n"]
     t0 = time.perf_counter()
     for _ in range(steps):
-        for name in ("so0n", "so1n"):
-            p, view = bufs[name]
-            check(lib.scg_euler_set(h, ids[name], p, view.size))
-        check(lib.scg_euler_march(h, 1))
+        check(lib.scg_euler_march_from_host(h, p0, v0.size, p1, v1.size, 1))
         check(lib.scg_euler_sync(h))
     t1 = time.perf_counter()
     for name in ("so0n", "so1n"):

@@ -225,6 +225,18 @@ int scg_euler_op(scg_euler * core, int op);
 /* march(steps): euler_march.cpp:350-359.  Asynchronous on the core's stream;
  * scg_euler_sync waits for it. */
 int scg_euler_march(scg_euler * core, int64_t steps);
+/* Not in the reference: scg_euler_set(SCG_EA_SO0N, so0n, n0),
+ * scg_euler_set(SCG_EA_SO1N, so1n, n1) and scg_euler_march(steps) in one call
+ * (the reference's array setters, wrap_multidim.cpp:381-408, then
+ * march).  When both tables are whole-array ranges of scg_host_alloc blocks
+ * the upload runs on a second stream in row chunks while the first substep
+ * marches the cells whose rows are already up; otherwise the tables are set
+ * as scg_euler_set does.  The state it leaves, and what a registered
+ * delivery receives, equal set + march bit for bit.  Asynchronous like
+ * scg_euler_march: the host tables must stay unchanged until scg_euler_sync
+ * returns. */
+int scg_euler_march_from_host(scg_euler * core, const double * so0n, int64_t n0, const double * so1n,
+                              int64_t n1, int64_t steps);
 int scg_euler_sync(scg_euler * core);
 /* Not in the reference: have every later march also leave array `which`
  * (SCG_EA_SO0N or SCG_EA_SO1N, the whole array of `count` doubles in the

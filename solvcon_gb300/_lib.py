@@ -73,6 +73,8 @@ _SIGS = {
     "scg_euler_normal_matrix": ([_vp, ctypes.c_int32, _vp], ctypes.c_int),
     "scg_euler_op": ([_vp, ctypes.c_int], ctypes.c_int),
     "scg_euler_march": ([_vp, ctypes.c_int64], ctypes.c_int),
+    "scg_euler_march_from_host": ([_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64,
+                                   ctypes.c_int64], ctypes.c_int),
     "scg_euler_sync": ([_vp], ctypes.c_int),
     "scg_euler_deliver": ([_vp, ctypes.c_int, _vp, ctypes.c_int64],
                           ctypes.c_int),

@@ -414,6 +414,28 @@ int scg_euler_march(scg_euler * core, int64_t steps)
     });
 }
 
+int scg_euler_march_from_host(scg_euler * core, const double * so0n, int64_t n0, const double * so1n,
+                              int64_t n1, int64_t steps)
+{
+    return guarded([&] {
+        auto * c = need(core, "scg_euler_march_from_host")->c.get();
+        if (steps < 0)
+        {
+            throw std::invalid_argument("EulerCore::march: steps must be >= 0");
+        }
+        if (!so0n || !so1n)
+        {
+            throw std::invalid_argument("scg_euler_march_from_host: null table");
+        }
+        if (n0 != c->array_size(scg::EA_SO0N) || n1 != c->array_size(scg::EA_SO1N))
+        {
+            throw std::invalid_argument("scg_euler_march_from_host: table sizes " + std::to_string(n0) + ", " +
+                                        std::to_string(n1) + " are not so0n's and so1n's");
+        }
+        c->march_from_host(so0n, so1n, steps);
+    });
+}
+
 int scg_euler_deliver(scg_euler * core, int which, double * host, int64_t count)
 {
     return guarded([&] { need(core, "scg_euler_deliver")->c->deliver(which, host, count); });

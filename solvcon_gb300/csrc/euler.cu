@@ -350,36 +350,82 @@ __global__ void k_get_field_host(R const * rec, double * out, int64_t nrow, int 
     }
 }
 
+// Two values per thread (grid-stride: a grid of one pass per pair is the
+// usual launch).
 template <int ND, typename R>
 __global__ void k_set_field_host(R * rec, double const * in, int64_t nrow, int off, int width, bool vec,
                                  Residual c)
 {
     int64_t const n = nrow * width;
-    int64_t const i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
-    if (i >= n)
+    int64_t const step = 2 * static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = 2 * (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x); i < n; i += step)
     {
-        return;
+        int64_t const r0 = i / width;
+        int const k0 = static_cast<int>(i - r0 * width);
+        if (i + 1 >= n)
+        {
+            field_store<ND, R>(rec, r0, off, k0, in[i], c);
+            continue;
+        }
+        double2 v;
+        if (vec)
+        {
+            v = *reinterpret_cast<double2 const *>(in + i);
+        }
+        else
+        {
+            v = make_double2(in[i], in[i + 1]);
+        }
+        int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
+        int const k1 = k0 + 1 < width ? k0 + 1 : 0;
+        field_store<ND, R>(rec, r0, off, k0, v.x, c);
+        field_store<ND, R>(rec, r1, off, k1, v.y, c);
     }
-    int64_t const r0 = i / width;
-    int const k0 = static_cast<int>(i - r0 * width);
-    if (i + 1 >= n)
+}
+
+// The highest row any cell of each chunk of csize cells reads in a substep
+// (its own row and its neighbours' over its cell type's faces), one block per
+// chunk: march_from_host launches a chunk's substep once those rows are up.
+__global__ void k_chunk_top_row(int32_t const * nbr, int8_t const * ctype, int64_t ncell, int64_t csize,
+                                int nslot, int64_t ngst, int64_t * top)
+{
+    __shared__ int64_t sh[256];
+    int64_t const c0 = static_cast<int64_t>(blockIdx.x) * csize;
+    int64_t const c1 = c0 + csize < ncell ? c0 + csize : ncell;
+    int64_t m = -1;
+    for (int64_t t = c0 + threadIdx.x; t < c1; t += blockDim.x)
     {
-        field_store<ND, R>(rec, r0, off, k0, in[i], c);
-        return;
+        int nf;
+        switch (ctype[t])
+        {
+        case CT_TRIANGLE: nf = 3; break;
+        case CT_QUAD: nf = 4; break;
+        case CT_TET: nf = 4; break;
+        case CT_HEX: nf = 6; break;
+        default: nf = 5; break; // prism, pyramid
+        }
+        nf = nf < nslot ? nf : nslot;
+        m = m > ngst + t ? m : ngst + t;
+        for (int f = 0; f < nf; ++f)
+        {
+            int64_t const j = nbr[static_cast<int64_t>(f) * ncell + t];
+            m = m > j ? m : j;
+        }
     }
-    double2 v;
-    if (vec)
+    sh[threadIdx.x] = m;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1)
     {
-        v = *reinterpret_cast<double2 const *>(in + i);
+        if (static_cast<int>(threadIdx.x) < k)
+        {
+            sh[threadIdx.x] = sh[threadIdx.x] > sh[threadIdx.x + k] ? sh[threadIdx.x] : sh[threadIdx.x + k];
+        }
+        __syncthreads();
     }
-    else
+    if (threadIdx.x == 0)
     {
-        v = make_double2(in[i], in[i + 1]);
+        top[blockIdx.x] = sh[0];
     }
-    int64_t const r1 = k0 + 1 < width ? r0 : r0 + 1;
-    int const k1 = k0 + 1 < width ? k0 + 1 : 0;
-    field_store<ND, R>(rec, r0, off, k0, v.x, c);
-    field_store<ND, R>(rec, r1, off, k1, v.y, c);
 }
 
 // so1n written from a mapped host table and then calc_solt of each row as
@@ -399,62 +445,66 @@ __global__ void __launch_bounds__(BLOCK) k_set_so1_host_solt(R * rec, double con
     constexpr int W = NEQ * ND;
     using RC = Rec<ND, R>;
     __shared__ double buf[BLOCK * W];
-    int64_t const r0 = static_cast<int64_t>(blockIdx.x) * BLOCK;
-    int64_t const left = nrow - r0;
-    int const nr = static_cast<int>(left < BLOCK ? left : BLOCK);
-    int const n = nr * W;
-    double const * const src = in + r0 * W;
-    for (int i = 2 * static_cast<int>(threadIdx.x); i < n; i += 2 * BLOCK)
+    // Grid-stride over stretches of BLOCK rows (see k_set_field_host).
+    for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * BLOCK; r0 < nrow;
+         r0 += static_cast<int64_t>(gridDim.x) * BLOCK)
     {
-        if (vec && i + 1 < n)
+        int64_t const left = nrow - r0;
+        int const nr = static_cast<int>(left < BLOCK ? left : BLOCK);
+        int const n = nr * W;
+        double const * const src = in + r0 * W;
+        __syncthreads(); // the previous stretch is done with buf
+        for (int i = 2 * static_cast<int>(threadIdx.x); i < n; i += 2 * BLOCK)
         {
-            double2 const v = *reinterpret_cast<double2 const *>(src + i);
-            buf[i] = v.x;
-            buf[i + 1] = v.y;
-        }
-        else
-        {
-            buf[i] = src[i];
-            if (i + 1 < n)
+            if (vec && i + 1 < n)
             {
-                buf[i + 1] = src[i + 1];
+                double2 const v = *reinterpret_cast<double2 const *>(src + i);
+                buf[i] = v.x;
+                buf[i + 1] = v.y;
+            }
+            else
+            {
+                buf[i] = src[i];
+                if (i + 1 < n)
+                {
+                    buf[i + 1] = src[i + 1];
+                }
             }
         }
-    }
-    __syncthreads();
-    if (static_cast<int>(threadIdx.x) >= nr)
-    {
-        return;
-    }
-    int64_t const r = r0 + threadIdx.x;
-    R * const row = rec + r * RC::RS;
-    R v[RC::NUSED];
+        __syncthreads();
+        if (static_cast<int>(threadIdx.x) < nr)
+        {
+            int64_t const r = r0 + threadIdx.x;
+            R * const row = rec + r * RC::RS;
+            R v[RC::NUSED];
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i)
-    {
-        v[i] = row[i];
-    }
+            for (int i = 0; i < NEQ; ++i)
+            {
+                v[i] = row[i];
+            }
 #pragma unroll
-    for (int k = 0; k < W; ++k)
-    {
-        v[2 * NEQ + k] = R(buf[threadIdx.x * W + k]);
-    }
-    Prim<ND, R> const q(v, gamma[r]);
-    R t[NEQ];
-    solt_prim<ND, R>(q, v, v + 2 * NEQ, t);
+            for (int k = 0; k < W; ++k)
+            {
+                v[2 * NEQ + k] = R(buf[threadIdx.x * W + k]);
+            }
+            Prim<ND, R> const q(v, gamma[r]);
+            R t[NEQ];
+            solt_prim<ND, R>(q, v, v + 2 * NEQ, t);
 #pragma unroll
-    for (int i = 0; i < NEQ; ++i)
-    {
-        row[NEQ + i] = t[i];
-    }
+            for (int i = 0; i < NEQ; ++i)
+            {
+                row[NEQ + i] = t[i];
+            }
 #pragma unroll
-    for (int k = 0; k < W; ++k)
-    {
-        row[2 * NEQ + k] = v[2 * NEQ + k];
-    }
-    if constexpr (RC::PRIM)
-    {
-        q.cache(row + RC::OP);
+            for (int k = 0; k < W; ++k)
+            {
+                row[2 * NEQ + k] = v[2 * NEQ + k];
+            }
+            if constexpr (RC::PRIM)
+            {
+                q.cache(row + RC::OP);
+            }
+        }
     }
 }
 
@@ -826,6 +876,27 @@ public:
             cudaStreamSynchronize(own_stream);
             cudaStreamDestroy(own_stream);
         }
+        if (m_xfer)
+        {
+            cudaStreamSynchronize(m_xfer);
+            cudaStreamDestroy(m_xfer);
+        }
+        if (m_side)
+        {
+            cudaStreamSynchronize(m_side);
+            cudaStreamDestroy(m_side);
+        }
+        if (m_cev)
+        {
+            cudaEventDestroy(m_cev);
+        }
+        for (auto & e : m_xev)
+        {
+            if (e)
+            {
+                cudaEventDestroy(e);
+            }
+        }
     }
 
     size_t device_bytes() const override
@@ -968,6 +1039,7 @@ public:
 
     void compact()
     {
+        m_plan.valid = false;
         if (ncell == 0)
         {
             return;
@@ -1394,25 +1466,35 @@ public:
     }
 
     // The fused kernel specialised to the mesh's cell type when it has only
-    // triangles or only tetrahedra (the simplex paths), else the generic one.
-    void launch_fused()
+    // triangles or only tetrahedra (the simplex paths), else the generic one,
+    // over rows [t0, t1) of its work order (body cells, then ghost rows).
+    void launch_fused(int64_t t0 = 0, int64_t t1 = -1)
     {
+        if (t1 < 0)
+        {
+            t1 = nrow;
+        }
+        if (t1 <= t0)
+        {
+            return;
+        }
+        unsigned const g = grid_for(t1 - t0);
         constexpr int SIMPLEX = (ND == 2) ? CT_TRIANGLE : CT_TET;
         if (single_ct == SIMPLEX)
         {
             constexpr int MINB = min_blocks<ND, R, SIMPLEX, BLOCK, G>();
             if constexpr (MINB > 0)
             {
-                k_fused_mb<ND, R, G, SIMPLEX, MINB><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+                k_fused_mb<ND, R, G, SIMPLEX, MINB><<<g, BLOCK, 0, stream>>>(args(), t0, t1);
             }
             else
             {
-                k_fused<ND, R, G, SIMPLEX><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+                k_fused<ND, R, G, SIMPLEX><<<g, BLOCK, 0, stream>>>(args(), t0, t1);
             }
         }
         else
         {
-            k_fused<ND, R, G><<<grid_for(nrow), BLOCK, 0, stream>>>(args());
+            k_fused<ND, R, G><<<g, BLOCK, 0, stream>>>(args(), t0, t1);
         }
     }
 
@@ -1432,24 +1514,211 @@ public:
             march_substep();
             m_deliver_now = false;
         }
-        if (!IN_KERNEL && delivers)
+        gather_delivery(delivers);
+        async_pending = steps > 0 && nrow > 0;
+    }
+
+    // FP32: the registered host blocks receive the state after the march.
+    void gather_delivery(bool delivers)
+    {
+        if (sizeof(R) == 8 || !delivers)
         {
-            for (int k = 0; k < 2; ++k)
+            return;
+        }
+        for (int k = 0; k < 2; ++k)
+        {
+            Delivery const & d = m_deliver[k];
+            if (d.host)
             {
-                Delivery const & d = m_deliver[k];
-                if (d.host)
-                {
-                    R * base;
-                    int off, width;
-                    field_of(k == 0 ? EA_SO0N : EA_SO1N, base, off, width);
-                    int64_t const n = static_cast<int64_t>(d.nbytes / sizeof(double));
-                    k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
-                        base, d.dev, nrow, off, width, true, so0_residual(k == 0 ? EA_SO0N : EA_SO1N));
-                    launched(stream, "get_field_host");
-                }
+                R * base;
+                int off, width;
+                field_of(k == 0 ? EA_SO0N : EA_SO1N, base, off, width);
+                int64_t const n = static_cast<int64_t>(d.nbytes / sizeof(double));
+                k_get_field_host<ND, R><<<grid_for((n + 1) / 2), BLOCK, 0, stream>>>(
+                    base, d.dev, nrow, off, width, true, so0_residual(k == 0 ? EA_SO0N : EA_SO1N));
+                launched(stream, "get_field_host");
             }
         }
-        async_pending = steps > 0 && nrow > 0;
+    }
+
+    // set_array(so0n), set_array(so1n) and march(steps), with the state's
+    // upload overlapped with the first substep when both tables lie in
+    // scg_host_alloc blocks (page-locked): the upload runs in row chunks on a
+    // second stream, and the first substep's fused kernel runs in the
+    // matching cell chunks, each after the upload of every row its cells read
+    // (the chunk plan).  Same values through the same kernels: the state it
+    // leaves is set + march's, bit for bit.
+    void march_from_host(double const * so0n, double const * so1n, int64_t steps) override
+    {
+        size_t const nb0 = sizeof(double) * static_cast<size_t>(array_size(EA_SO0N));
+        size_t const nb1 = sizeof(double) * static_cast<size_t>(array_size(EA_SO1N));
+        double const * const d0 = static_cast<double const *>(mapped_host(so0n, nb0));
+        double const * const d1 = static_cast<double const *>(mapped_host(so1n, nb1));
+        // FP32: the march takes a fraction of the link's time, so there is
+        // nothing to hide the upload under (set_array's mapped scatter is the
+        // faster route).
+        if (!d0 || !d1 || steps <= 0 || ncell == 0 || sizeof(R) == 4)
+        {
+            set_array(EA_SO0N, so0n);
+            set_array(EA_SO1N, so1n);
+            march(steps);
+            return;
+        }
+        upload_bc();
+        bool const delivers = revalidate_delivery();
+        constexpr bool IN_KERNEL = sizeof(R) == 8;
+        plan_chunks();
+        int const nch = m_plan.nch;
+        // The upload: the copy engine moves each chunk's rows of the two
+        // pinned tables into a device table (no SM takes part, so the
+        // substep marches beside it), and a scatter at HBM speed puts them
+        // into the records, so0t made on the way, as set_array does for a
+        // mapped table.
+        constexpr int W = NEQ * ND;
+        double * const st0 = staging(nrow * (NEQ + W));
+        double * const st1 = st0 + nrow * NEQ;
+        // The records it writes may still be read by work queued on the
+        // core's stream (an earlier march): that goes first.
+        cuda_check(cudaEventRecord(m_xev[XCH], stream), "record");
+        cuda_check(cudaStreamWaitEvent(m_xfer, m_xev[XCH], 0), "wait");
+        R * base;
+        int off, width;
+        field_of(EA_SO0N, base, off, width);
+        bool const solt = tbuf != (cur ^ 1);
+        Residual const c = so0_written(EA_SO0N);
+        for (int j = 0; j < nch; ++j)
+        {
+            int64_t const r0 = j == 0 ? 0 : ngstcell + m_plan.cell[j];
+            int64_t const r1 = ngstcell + m_plan.cell[j + 1];
+            int64_t const nr = r1 - r0;
+            double * const in0 = st0 + r0 * NEQ;
+            double * const in1 = st1 + r0 * W;
+            cuda_check(cudaMemcpyAsync(in0, so0n + r0 * NEQ, sizeof(double) * static_cast<size_t>(nr * NEQ),
+                                       cudaMemcpyHostToDevice, m_xfer),
+                       "H2D");
+            cuda_check(cudaMemcpyAsync(in1, so1n + r0 * W, sizeof(double) * static_cast<size_t>(nr * W),
+                                       cudaMemcpyHostToDevice, m_xfer),
+                       "H2D");
+            k_set_field_host<ND, R><<<grid_for((nr * NEQ + 1) / 2), BLOCK, 0, m_xfer>>>(
+                base + r0 * RS, in0, nr, 0, NEQ, reinterpret_cast<uintptr_t>(in0) % 16 == 0,
+                Residual{c.comp, c.ngst - r0, c.ncell});
+            launched(m_xfer, "set_field_host");
+            if (solt)
+            {
+                k_set_so1_host_solt<ND, R><<<grid_for(nr), BLOCK, 0, m_xfer>>>(
+                    base + r0 * RS, in1, d_gamma.ptr + r0, nr, reinterpret_cast<uintptr_t>(in1) % 16 == 0);
+                launched(m_xfer, "set_so1_host_solt");
+            }
+            else
+            {
+                k_set_field_host<ND, R><<<grid_for((nr * W + 1) / 2), BLOCK, 0, m_xfer>>>(
+                    base + r0 * RS, in1, nr, 2 * NEQ, W, reinterpret_cast<uintptr_t>(in1) % 16 == 0, Residual{});
+                launched(m_xfer, "set_field_host");
+            }
+            cuda_check(cudaEventRecord(m_xev[j], m_xfer), "record");
+        }
+        // What the two sets leave behind.
+        next_valid = solt;
+        next_buf = cur ^ 1;
+        // The first substep, as march_substep with its fused launch in
+        // chunks.
+        comp_ready();
+        cur ^= 1;
+        if (next_valid && next_buf == cur)
+        {
+            tbuf = cur;
+        }
+        else
+        {
+            cuda_check(cudaStreamWaitEvent(stream, m_xev[nch - 1], 0), "wait");
+            run_solt();
+        }
+        m_deliver_now = false;
+        // The chunks write disjoint rows, so they alternate between the
+        // core's stream and a second one: a chunk's last partial wave
+        // overlaps the next chunk instead of idling SMs.
+        cuda_check(cudaEventRecord(m_cev, stream), "record");
+        cuda_check(cudaStreamWaitEvent(m_side, m_cev, 0), "wait");
+        cudaStream_t const mine = stream;
+        for (int k = 0; k < nch; ++k)
+        {
+            stream = (k & 1) ? m_side : mine;
+            cuda_check(cudaStreamWaitEvent(stream, m_xev[m_plan.need[k]], 0), "wait");
+            launch_fused(m_plan.cell[k], m_plan.cell[k + 1]);
+            launched(stream, "fused_substep");
+        }
+        stream = mine;
+        cuda_check(cudaEventRecord(m_cev, m_side), "record");
+        cuda_check(cudaStreamWaitEvent(stream, m_cev, 0), "wait");
+        cuda_check(cudaStreamWaitEvent(stream, m_xev[nch - 1], 0), "wait");
+        if (ngstcell > 0)
+        {
+            launch_fused(ncell, nrow); // ghost rows without a boundary condition
+            launched(stream, "fused_substep");
+        }
+        next_valid = true;
+        next_buf = cur ^ 1;
+        // Its second substep and the remaining steps.
+        m_deliver_now = IN_KERNEL && delivers && steps == 1;
+        march_substep();
+        m_deliver_now = false;
+        for (int64_t s = 1; s < steps; ++s)
+        {
+            march_substep();
+            m_deliver_now = IN_KERNEL && delivers && s + 1 == steps;
+            march_substep();
+            m_deliver_now = false;
+        }
+        gather_delivery(delivers);
+        async_pending = true;
+    }
+
+    // Cell chunks of the overlapped first substep and, for each, the last
+    // upload chunk it must wait for: the one holding the highest row any of
+    // its cells reads (its own rows and its neighbours'; ghost rows lie in
+    // upload chunk 0).  Made once per mesh on the device.
+    void plan_chunks()
+    {
+        if (m_plan.valid)
+        {
+            return;
+        }
+        if (!m_xfer)
+        {
+            cuda_check(cudaStreamCreateWithFlags(&m_xfer, cudaStreamNonBlocking), "cudaStreamCreate");
+            cuda_check(cudaStreamCreateWithFlags(&m_side, cudaStreamNonBlocking), "cudaStreamCreate");
+            cuda_check(cudaEventCreateWithFlags(&m_cev, cudaEventDisableTiming), "event");
+            for (auto & e : m_xev)
+            {
+                cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            }
+        }
+        int64_t nch = ncell / 65536;
+        nch = nch < 1 ? 1 : (nch > XCH ? XCH : nch);
+        int64_t csize = (ncell + nch - 1) / nch;
+        csize = (csize + BLOCK - 1) / BLOCK * BLOCK;
+        nch = (ncell + csize - 1) / csize;
+        m_plan.nch = static_cast<int>(nch);
+        for (int64_t k = 0; k <= nch; ++k)
+        {
+            m_plan.cell[k] = k * csize < ncell ? k * csize : ncell;
+        }
+        DevBuf<int64_t> top(static_cast<size_t>(nch));
+        k_chunk_top_row<<<static_cast<unsigned>(nch), 256, 0, stream>>>(d_nbr.ptr, d_ctype.ptr, ncell, csize,
+                                                                          std::max(nslot, 1), ngstcell, top.ptr);
+        launched(stream, "chunk_top_row");
+        int64_t h[XCH];
+        cuda_check(cudaMemcpyAsync(h, top.ptr, sizeof(int64_t) * static_cast<size_t>(nch), cudaMemcpyDeviceToHost,
+                                   stream),
+                   "D2H");
+        sync();
+        for (int64_t k = 0; k < nch; ++k)
+        {
+            int64_t const r = h[k] - ngstcell; // a body cell, or < 0: a ghost row
+            int64_t const j = r < 0 ? 0 : r / csize;
+            m_plan.need[k] = static_cast<int>(std::max(k, std::min(j, nch - 1)));
+        }
+        m_plan.valid = true;
     }
 
     bool delivering() override { return revalidate_delivery(); }
@@ -1662,6 +1931,20 @@ private:
     int64_t nrow = 0;
     int nslot = 0;
     cudaStream_t own_stream = nullptr;
+    // march_from_host: the upload stream, an event per upload chunk (and one
+    // for the start), and the chunk plan.
+    static constexpr int XCH = 16;
+    cudaStream_t m_xfer = nullptr;
+    cudaStream_t m_side = nullptr; // the second stream of the chunked substep
+    cudaEvent_t m_cev = nullptr;
+    cudaEvent_t m_xev[XCH + 1] = {};
+    struct ChunkPlan
+    {
+        bool valid = false;
+        int nch = 0;
+        int64_t cell[XCH + 1] = {};
+        int need[XCH] = {};
+    } m_plan;
     cudaStream_t stream = nullptr;
     MeshView mv{};
 

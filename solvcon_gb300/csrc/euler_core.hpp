@@ -114,6 +114,10 @@ public:
     virtual void init_solution(double gamma, double rho, double const * v, double p) = 0;
     virtual void op(int which) = 0;
     virtual void march(int64_t steps) = 0;
+    // set_array(EA_SO0N, so0n), set_array(EA_SO1N, so1n), march(steps), with
+    // the upload overlapped with the first substep when both tables are
+    // whole-array ranges of scg_host_alloc blocks.
+    virtual void march_from_host(double const * so0n, double const * so1n, int64_t steps) = 0;
     // Have every later march also leave array `which` (EA_SO0N or EA_SO1N)
     // of its last substep in the host block `host` (a whole-array, 16-byte
     // aligned range of one scg_host_alloc block): written by the last FP64

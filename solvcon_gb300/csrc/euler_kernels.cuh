@@ -1210,11 +1210,18 @@ __device__ __forceinline__ void fused_thread(MarchArgs<R, G> const & a, int64_t 
     }
 }
 
+// One substep over the rows [t0, t1) of the work order (body cells 0 ..
+// ncell - 1, then the ghost rows): the whole substep is [0, ncell + ngst);
+// a march that overlaps its state's upload with its first substep launches
+// it in ranges.
 template <int ND, typename R, typename G, int CT1 = 0>
-__global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
+__global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a, int64_t t0, int64_t t1)
 {
-    fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(
-        a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    int64_t const t = t0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t < t1)
+    {
+        fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(a, t);
+    }
 }
 
 // The same kernel asking the compiler for MINB resident blocks of 128
@@ -1222,10 +1229,13 @@ __global__ void __launch_bounds__(128) k_fused(MarchArgs<R, G> a)
 // up to 255 registers, so the kernels that do not carry keep the one-argument
 // bound.
 template <int ND, typename R, typename G, int CT1, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_fused_mb(MarchArgs<R, G> a)
+__global__ void __launch_bounds__(128, MINB) k_fused_mb(MarchArgs<R, G> a, int64_t t0, int64_t t1)
 {
-    fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(
-        a, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    int64_t const t = t0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t < t1)
+    {
+        fused_thread<ND, R, G, CT1, carry_shared<ND>() ? 128 : 0>(a, t);
+    }
 }
 
 } // namespace dev

@@ -277,3 +277,124 @@ def test_batched_march_refuses_a_delivering_core():
                                   before)
     finally:
         blk.free()
+
+
+def _chunked_core(precision, kind):
+    """A core large enough for several upload chunks (65,536 cells each), a
+    quadrilateral one (the generic kernel, one chunk), or one whose cells
+    are numbered at random (every chunk then needs the whole upload); half
+    of the boundary faces carry a slip wall, so ghost rows without a
+    condition are marched too."""
+    import solvcon_gb300 as sg
+    from solvcon_gb300 import meshgen
+    if kind == "tet":
+        x, t, c = meshgen.tet_cube(28, 0.15, 3)
+        ndim = 3
+    elif kind == "quad":
+        x, t, c = meshgen.quad_square(40, 0.15, 2)
+        ndim = 2
+    else:
+        x, t, c = meshgen.tri_square(260, 0.2, 3)
+        ndim = 2
+        if kind == "shuffled":
+            perm = np.random.default_rng(9).permutation(len(t))
+            t, c = t[perm], c[perm]
+    mesh = meshgen.build_mesh(ndim, x, t, c)
+    ec = sg.EulerCore(mesh=mesh, time_increment=1e-3 if ndim == 2 else 5e-4,
+                      precision=precision)
+    clcnd = np.array(mesh.clcnd.ndarray)[mesh.ngstcell:]
+    state = (meshgen.quadrant_state(clcnd, seed=5) if ndim == 2
+             else meshgen.blast_state(clcnd))
+    ec.add_slipwall([int(f) for f in mesh.bndfcs.ndarray[::2, 0]])
+    meshgen.set_state(ec, mesh, state, 1.4)
+    ec.march(2)
+    ec.release_views()
+    return ec
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("kind", ["tri", "tet", "quad", "shuffled"])
+def test_march_from_host_equals_set_and_march(precision, kind):
+    """scg_euler_march_from_host overlaps the upload of the state from host
+    blocks with the first substep, in chunks; what it leaves (the tables,
+    the delivered blocks, and a march continued from it) equals
+    scg_euler_set(so0n), scg_euler_set(so1n), scg_euler_march bit for
+    bit."""
+    from solvcon_gb300._lib import check, lib
+    cores = [_chunked_core(precision, kind) for _ in range(2)]
+    shapes = {n: _shape(cores[0], n) for n in ("so0n", "so1n")}
+    rng = np.random.default_rng(4)
+    start = {n: _get(cores[0], RECORD_TABLES[n], shapes[n]) *
+             (1 + 1e-6 * rng.uniform(-1, 1, shapes[n])) for n in shapes}
+    blocks = []
+    try:
+        ins, outs = [], []
+        for ec in cores:
+            inp, out = {}, {}
+            for n, shape in shapes.items():
+                size = int(np.prod(shape))
+                bi, bo = _Block(size), _Block(size)
+                blocks += [bi, bo]
+                bo.view[...] = np.nan
+                check(lib.scg_euler_deliver(ec.handle, RECORD_TABLES[n],
+                                            ctypes.c_void_p(bo.addr), size))
+                inp[n], out[n] = bi, bo
+            ins.append(inp)
+            outs.append(out)
+        for steps in (1, 3):
+            for inp in ins:
+                for n in shapes:
+                    inp[n].view[...] = start[n].ravel()
+            a, b = cores
+            for n in ("so0n", "so1n"):
+                check(lib.scg_euler_set(a.handle, RECORD_TABLES[n],
+                                        ctypes.c_void_p(ins[0][n].addr),
+                                        ins[0][n].view.size))
+            check(lib.scg_euler_march(a.handle, steps))
+            check(lib.scg_euler_sync(a.handle))
+            check(lib.scg_euler_march_from_host(
+                b.handle, ctypes.c_void_p(ins[1]["so0n"].addr),
+                ins[1]["so0n"].view.size, ctypes.c_void_p(ins[1]["so1n"].addr),
+                ins[1]["so1n"].view.size, steps))
+            check(lib.scg_euler_sync(b.handle))
+            for n, shape in shapes.items():
+                np.testing.assert_array_equal(
+                    _get(b, RECORD_TABLES[n], shape),
+                    _get(a, RECORD_TABLES[n], shape), err_msg=n)
+                np.testing.assert_array_equal(outs[1][n].view, outs[0][n].view,
+                                              err_msg=n)
+            for ec in cores:
+                check(lib.scg_euler_march(ec.handle, 1))
+                check(lib.scg_euler_sync(ec.handle))
+            for n, shape in shapes.items():
+                np.testing.assert_array_equal(
+                    _get(b, RECORD_TABLES[n], shape),
+                    _get(a, RECORD_TABLES[n], shape), err_msg=n + " after")
+        for ec in cores:
+            for n in shapes:
+                check(lib.scg_euler_deliver(ec.handle, RECORD_TABLES[n], None, 0))
+    finally:
+        for blk in blocks:
+            blk.free()
+
+
+def test_march_from_host_pageable_tables_and_bad_sizes():
+    """Tables outside scg_host_alloc blocks are set as scg_euler_set sets
+    them (same result as set + march); wrong sizes raise ValueError."""
+    from solvcon_gb300._lib import check, lib, ptr
+    a, b = (_chunked_core("fp64", "quad") for _ in range(2))
+    so0 = _get(a, RECORD_TABLES["so0n"], _shape(a, "so0n")) * 1.000001
+    so1 = _get(a, RECORD_TABLES["so1n"], _shape(a, "so1n"))
+    check(lib.scg_euler_set(a.handle, RECORD_TABLES["so0n"], ptr(so0), so0.size))
+    check(lib.scg_euler_set(a.handle, RECORD_TABLES["so1n"], ptr(so1), so1.size))
+    check(lib.scg_euler_march(a.handle, 2))
+    check(lib.scg_euler_sync(a.handle))
+    check(lib.scg_euler_march_from_host(b.handle, ptr(so0), so0.size, ptr(so1),
+                                        so1.size, 2))
+    check(lib.scg_euler_sync(b.handle))
+    for n in ("so0n", "so1n"):
+        np.testing.assert_array_equal(_get(b, RECORD_TABLES[n], _shape(b, n)),
+                                      _get(a, RECORD_TABLES[n], _shape(a, n)))
+    with pytest.raises(ValueError):
+        check(lib.scg_euler_march_from_host(b.handle, ptr(so0), so0.size - 1,
+                                            ptr(so1), so1.size, 1))
