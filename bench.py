@@ -1275,7 +1275,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-headline", action="store_true",
-                    help="default line: skip the batched and served figures")
+                    help="default line (the plain 2M-triangle workload): skip "
+                         "the batched and served figures")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cases", default=None,
                     help="accuracy workload: comma-separated subset of "
@@ -1384,6 +1385,7 @@ def main():
 
     headline = {}
     if (rank == 0 and world == 1 and args.workload == "tri2d"
+            and args.precision is None and args.nside is None
             and not args.no_headline):
         del core
         headline = headline_figures(local)
