@@ -58,7 +58,24 @@ struct E1DArgs
     R * cfl;
     int64_t n;
     double hdt, qdt;
+    // 1 / (x[i + 1] - x[i]) and 1 / (x[i + 2] - x[i]): the divisions of a
+    // half step that depend on the grid alone, formed once per coordinate
+    // write by the same expressions (so the same bits) instead of every
+    // half step.
+    double const * invdx;
+    double const * invd2;
 };
+
+// The grid's reciprocal tables of E1DArgs.
+__global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, double * invd2)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        invdx[i] = i + 1 < n ? 1.0 / (coord[i + 1] - coord[i]) : 0.0;
+        invd2[i] = i + 2 < n ? 1.0 / (coord[i + 2] - coord[i]) : 0.0;
+    }
+}
 
 // The solution-element kernel at point ic (Euler1DKernel::set_value and
 // derive, Euler1DCore.hpp:193-244): flux f, temporal derivatives ut, ft and
@@ -200,7 +217,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                 s_lr[threadIdx.x][i] = k.lr[i];
                 s_up[threadIdx.x][i] = k.up[i];
             }
-            s_idxr[threadIdx.x] = R(1.0 / (k.x - k.xneg));
+            s_idxr[threadIdx.x] = R(a.invdx[start + 2 * j - 1]);
         }
         if (threadIdx.x == 0)
         {
@@ -214,7 +231,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                     s_lr[B1D][i] = h.lr[i];
                     s_up[B1D][i] = h.up[i];
                 }
-                s_idxr[B1D] = R(1.0 / (h.x - h.xneg));
+                s_idxr[B1D] = R(a.invdx[start + 2 * jh - 1]);
             }
         }
         __syncthreads();
@@ -224,7 +241,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
             R v[3];
             if (DO_SO0)
             {
-                R const idx = R(1.0 / (a.coord[ic + 2] - a.coord[ic]));
+                R const idx = R(a.invd2[ic]);
                 for (int i = 0; i < 3; ++i)
                 {
                     v[i] = (k.ll[i] + s_lr[threadIdx.x + 1][i]) * idx;
@@ -244,7 +261,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
             }
             if constexpr (ALPHA > 0)
             {
-                R const idn = R(1.0 / (k.xpos - k.x));
+                R const idn = R(a.invdx[ic]);
                 R const idp = s_idxr[threadIdx.x + 1];
                 for (int i = 0; i < 3; ++i)
                 {
@@ -332,6 +349,8 @@ public:
         }
         scg::cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
         coord.alloc(static_cast<size_t>(n));
+        invdx.alloc(static_cast<size_t>(n));
+        invd2.alloc(static_cast<size_t>(n));
         for (auto * b : {&cfl, &gamma})
             b->alloc(static_cast<size_t>(n));
         so0.alloc(static_cast<size_t>(n * 3));
@@ -362,6 +381,8 @@ public:
         scg::cuda_check(cudaMemcpyAsync(c->coord.ptr, coord.ptr, sizeof(double) * static_cast<size_t>(n),
                                         cudaMemcpyDeviceToDevice, stream),
                         "copy");
+        sync();
+        c->spacing();
         for (int k = 1; k < 5; ++k)
         {
             size_t const cnt = static_cast<size_t>(count(k));
@@ -406,15 +427,24 @@ public:
         if (which == 0)
         {
             put(coord.ptr, host, cnt);
+            spacing();
             return;
         }
         put(state(which), host, cnt);
     }
 
+    // The grid's reciprocal tables from the coordinates.
+    void spacing()
+    {
+        k_inv_spacing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(coord.ptr, n, invdx.ptr, invd2.ptr);
+        scg::launched(stream, "e1d_inv_spacing");
+        sync();
+    }
+
     E1DArgs<R> args()
     {
         return E1DArgs<R>{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
-                          time_increment / 4.0};
+                          time_increment / 4.0, invdx.ptr, invd2.ptr};
     }
 
     // Loop bounds of a half step (Euler1DCore.cpp:73-74, 99-100).
@@ -571,6 +601,7 @@ private:
     }
 
     scg::DevBuf<double> coord;
+    scg::DevBuf<double> invdx, invd2; // see E1DArgs
     scg::DevBuf<R> cfl, so0, so1, gamma;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
