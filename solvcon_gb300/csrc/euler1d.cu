@@ -64,16 +64,40 @@ struct E1DArgs
     // half step.
     double const * invdx;
     double const * invd2;
+    // The solution element's offsets from the grid alone, [5][n]: x - xctr,
+    // xpos - x, (x + xpos) / 2 - xctr, x - xneg, (x + xneg) / 2 - xctr with
+    // xctr = (xpos + xneg) / 2 (Euler1DCore.hpp:210-244), formed once per
+    // coordinate write.
+    double const * seo;
 };
 
-// The grid's reciprocal tables of E1DArgs.
-__global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, double * invd2)
+// The grid's tables of E1DArgs.  The offsets round every operation on its
+// own (no contraction), so their bits do not depend on the kernel that
+// forms them.
+__global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, double * invd2, double * seo)
 {
     int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n)
     {
         invdx[i] = i + 1 < n ? 1.0 / (coord[i + 1] - coord[i]) : 0.0;
         invd2[i] = i + 2 < n ? 1.0 / (coord[i + 2] - coord[i]) : 0.0;
+        double o[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (i > 0 && i + 1 < n)
+        {
+            double const x = coord[i];
+            double const xneg = coord[i - 1];
+            double const xpos = coord[i + 1];
+            double const xctr = __dmul_rn(__dadd_rn(xpos, xneg), 0.5);
+            o[0] = __dsub_rn(x, xctr);
+            o[1] = __dsub_rn(xpos, x);
+            o[2] = __dsub_rn(__dmul_rn(0.5, __dadd_rn(x, xpos)), xctr);
+            o[3] = __dsub_rn(x, xneg);
+            o[4] = __dsub_rn(__dmul_rn(0.5, __dadd_rn(x, xneg)), xctr);
+        }
+        for (int k = 0; k < 5; ++k)
+        {
+            seo[k * n + i] = o[k];
+        }
     }
 }
 
@@ -85,7 +109,6 @@ __global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, d
 template <typename R>
 struct K1D
 {
-    double x, xneg, xpos;
     R r; // 1 / (rho + tiny), shared with update_cfl at the same point
     R up[3];
     R ll[3]; // flux through the lower-left of the CE to the right
@@ -96,10 +119,6 @@ template <typename R>
 __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> & k)
 {
     R const ga = a.gamma[ic];
-    k.x = a.coord[ic];
-    k.xneg = a.coord[ic - 1];
-    k.xpos = a.coord[ic + 1];
-    double const xctr = (k.xpos + k.xneg) * 0.5;
     R u[3], ux[3];
     for (int i = 0; i < 3; ++i)
     {
@@ -133,11 +152,11 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
         ft[i] = jac[i][0] * ut[0] + jac[i][1] * ut[1] + jac[i][2] * ut[2];
     }
     R const hdt = R(a.hdt), qdt = R(a.qdt);
-    R const dxctr = R(k.x - xctr);
-    R const dxl = R(k.xpos - k.x);
-    R const dml = R(0.5 * (k.x + k.xpos) - xctr);
-    R const dxr = R(k.x - k.xneg);
-    R const dmr = R(0.5 * (k.x + k.xneg) - xctr);
+    R const dxctr = R(a.seo[0 * a.n + ic]);
+    R const dxl = R(a.seo[1 * a.n + ic]);
+    R const dml = R(a.seo[2 * a.n + ic]);
+    R const dxr = R(a.seo[3 * a.n + ic]);
+    R const dmr = R(a.seo[4 * a.n + ic]);
     for (int i = 0; i < 3; ++i)
     {
         k.up[i] = u[i] + dxctr * ux[i] + hdt * ut[i];
@@ -351,6 +370,7 @@ public:
         coord.alloc(static_cast<size_t>(n));
         invdx.alloc(static_cast<size_t>(n));
         invd2.alloc(static_cast<size_t>(n));
+        seo.alloc(static_cast<size_t>(5 * n));
         for (auto * b : {&cfl, &gamma})
             b->alloc(static_cast<size_t>(n));
         so0.alloc(static_cast<size_t>(n * 3));
@@ -433,10 +453,11 @@ public:
         put(state(which), host, cnt);
     }
 
-    // The grid's reciprocal tables from the coordinates.
+    // The grid's tables (E1DArgs) from the coordinates.
     void spacing()
     {
-        k_inv_spacing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(coord.ptr, n, invdx.ptr, invd2.ptr);
+        k_inv_spacing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(coord.ptr, n, invdx.ptr, invd2.ptr,
+                                                                                   seo.ptr);
         scg::launched(stream, "e1d_inv_spacing");
         sync();
     }
@@ -444,7 +465,7 @@ public:
     E1DArgs<R> args()
     {
         return E1DArgs<R>{coord.ptr, gamma.ptr, so0.ptr, so1.ptr, cfl.ptr, n, time_increment / 2.0,
-                          time_increment / 4.0, invdx.ptr, invd2.ptr};
+                          time_increment / 4.0, invdx.ptr, invd2.ptr, seo.ptr};
     }
 
     // Loop bounds of a half step (Euler1DCore.cpp:73-74, 99-100).
@@ -601,7 +622,7 @@ private:
     }
 
     scg::DevBuf<double> coord;
-    scg::DevBuf<double> invdx, invd2; // see E1DArgs
+    scg::DevBuf<double> invdx, invd2, seo; // see E1DArgs
     scg::DevBuf<R> cfl, so0, so1, gamma;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_alpha = 0;
