@@ -398,3 +398,44 @@ def test_march_from_host_pageable_tables_and_bad_sizes():
     with pytest.raises(ValueError):
         check(lib.scg_euler_march_from_host(b.handle, ptr(so0), so0.size - 1,
                                             ptr(so1), so1.size, 1))
+
+
+def test_march_from_host_on_a_caller_stream():
+    """With the core on a stream of the caller's (scg_euler_set_stream), the
+    chunked first substep runs on that stream and a second one, joined back
+    onto the caller's before the call's later work: the result still equals
+    set + march on the core's own stream."""
+    torch = pytest.importorskip("torch")
+    from solvcon_gb300._lib import check, lib
+    a, b = (_chunked_core("fp64", "tri") for _ in range(2))
+    shapes = {n: _shape(a, n) for n in ("so0n", "so1n")}
+    start = {n: _get(a, RECORD_TABLES[n], shapes[n]) * 1.000001
+             for n in shapes}
+    blocks = {}
+    stream = torch.cuda.Stream()
+    try:
+        check(lib.scg_euler_set_stream(b.handle,
+                                       ctypes.c_void_p(stream.cuda_stream)))
+        for n, shape in shapes.items():
+            blocks[n] = _Block(int(np.prod(shape)))
+            blocks[n].view[...] = start[n].ravel()
+        for n in shapes:
+            check(lib.scg_euler_set(a.handle, RECORD_TABLES[n],
+                                    ctypes.c_void_p(blocks[n].addr),
+                                    blocks[n].view.size))
+        check(lib.scg_euler_march(a.handle, 2))
+        check(lib.scg_euler_sync(a.handle))
+        check(lib.scg_euler_march_from_host(
+            b.handle, ctypes.c_void_p(blocks["so0n"].addr),
+            blocks["so0n"].view.size, ctypes.c_void_p(blocks["so1n"].addr),
+            blocks["so1n"].view.size, 2))
+        check(lib.scg_euler_sync(b.handle))
+        stream.synchronize()
+        for n, shape in shapes.items():
+            np.testing.assert_array_equal(_get(b, RECORD_TABLES[n], shape),
+                                          _get(a, RECORD_TABLES[n], shape),
+                                          err_msg=n)
+        check(lib.scg_euler_set_stream(b.handle, None))
+    finally:
+        for blk in blocks.values():
+            blk.free()
