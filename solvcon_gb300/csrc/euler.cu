@@ -1640,14 +1640,22 @@ public:
         cuda_check(cudaEventRecord(m_cev, stream), "record");
         cuda_check(cudaStreamWaitEvent(m_side, m_cev, 0), "wait");
         cudaStream_t const mine = stream;
-        for (int k = 0; k < nch; ++k)
         {
-            stream = (k & 1) ? m_side : mine;
-            cuda_check(cudaStreamWaitEvent(stream, m_xev[m_plan.need[k]], 0), "wait");
-            launch_fused(m_plan.cell[k], m_plan.cell[k + 1]);
-            launched(stream, "fused_substep");
+            // The core's stream is back to its own even if a launch throws.
+            struct Restore
+            {
+                cudaStream_t & s;
+                cudaStream_t v;
+                ~Restore() { s = v; }
+            } const restore{stream, mine};
+            for (int k = 0; k < nch; ++k)
+            {
+                stream = (k & 1) ? m_side : mine;
+                cuda_check(cudaStreamWaitEvent(stream, m_xev[m_plan.need[k]], 0), "wait");
+                launch_fused(m_plan.cell[k], m_plan.cell[k + 1]);
+                launched(stream, "fused_substep");
+            }
         }
-        stream = mine;
         cuda_check(cudaEventRecord(m_cev, m_side), "record");
         cuda_check(cudaStreamWaitEvent(stream, m_cev, 0), "wait");
         cuda_check(cudaStreamWaitEvent(stream, m_xev[nch - 1], 0), "wait");
