@@ -11,6 +11,7 @@ library raises ImportError.
 from .buffer import SimpleArray  # noqa: F401
 from .mesh import Gmsh, Plot3d, StaticMesh, StaticMeshBc  # noqa: F401
 from .multidim import EulerCore, GradientElement  # noqa: F401
+from .host import HostTable  # noqa: F401
 from .field import EulerField  # noqa: F401
 
 __version__ = "0.1.0"

@@ -259,6 +259,54 @@ class EulerCore:
     def sync(self):
         check(lib.scg_euler_sync(self._h))
 
+    # -- host tables exchanged every step (not in the reference) -------------
+
+    def host_table(self, name):
+        """A :class:`~solvcon_gb300.host.HostTable` shaped for array ``name``
+        (``"so0n"``, ``"so1n"``, ...), ghost rows first."""
+        from .host import HostTable
+        shape, _ = self._shape(_ID[name])
+        return HostTable(shape)
+
+    def deliver(self, so0n=None, so1n=None):
+        """Have every later march leave its new so0n / so1n in these
+        :class:`~solvcon_gb300.host.HostTable` objects (None: stop), as it
+        computes them (FP64) or right after (FP32); scg_euler_deliver."""
+        for name, t in (("so0n", so0n), ("so1n", so1n)):
+            if t is None:
+                check(lib.scg_euler_deliver(self._h, _ID[name], None, 0))
+            else:
+                check(lib.scg_euler_deliver(self._h, _ID[name],
+                                            ctypes.c_void_p(t.address), t.size))
+
+    def march_from_host(self, so0n, so1n, steps):
+        """Set so0n and so1n from host tables and advance ``steps`` full
+        steps, waiting for the device; with :class:`HostTable` tables the
+        upload runs while the first substep already marches the cells whose
+        rows are up (scg_euler_march_from_host).  Same state as setting the
+        two arrays and calling :meth:`march`, bit for bit."""
+        tabs = []
+        for name, t in (("so0n", so0n), ("so1n", so1n)):
+            shape, _ = self._shape(_ID[name])
+            if hasattr(t, "address"):
+                if tuple(t.shape) != tuple(shape):
+                    raise ValueError("EulerCore.march_from_host: %s has shape "
+                                     "%s, not %s" % (name, t.shape, shape))
+                tabs.append((ctypes.c_void_p(t.address), t.size))
+            else:
+                arr = np.ascontiguousarray(t, dtype="float64")
+                if arr.shape != tuple(shape):
+                    raise ValueError("EulerCore.march_from_host: %s has shape "
+                                     "%s, not %s" % (name, arr.shape, shape))
+                tabs.append((ptr(arr), arr.size, arr))
+        self._flush()
+        check(lib.scg_euler_march_from_host(self._h, tabs[0][0], tabs[0][1],
+                                            tabs[1][0], tabs[1][1], int(steps)))
+        self._valid.clear()
+        self.sync()
+        if self._exposed:
+            self._after(0)
+
     def set_stream(self, cuda_stream):
         """Run on a caller-owned cudaStream_t (an int address or None)."""
         check(lib.scg_euler_set_stream(self._h, ctypes.c_void_p(

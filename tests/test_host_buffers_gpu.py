@@ -439,3 +439,36 @@ def test_march_from_host_on_a_caller_stream():
     finally:
         for blk in blocks.values():
             blk.free()
+
+
+def test_python_host_tables_deliver_and_march_from_host():
+    """The same route from Python: HostTable state fed to
+    EulerCore.march_from_host and read back through EulerCore.deliver gives
+    the state of setting the arrays and calling march."""
+    import solvcon_gb300 as sg
+    a, b = (_chunked_core("fp64", "tri") for _ in range(2))
+    start = {n: np.array(getattr(a, n).ndarray) * 1.000001
+             for n in ("so0n", "so1n")}
+    ins = {n: b.host_table(n) for n in start}
+    outs = {n: b.host_table(n) for n in start}
+    try:
+        assert isinstance(ins["so0n"], sg.HostTable)
+        for n in start:
+            ins[n].array[...] = start[n]
+            outs[n].array[...] = np.nan
+            getattr(a, n).ndarray[...] = start[n]
+        a.release_views()
+        a.march(2)
+        b.deliver(so0n=outs["so0n"], so1n=outs["so1n"])
+        b.march_from_host(ins["so0n"], ins["so1n"], 2)
+        for n in start:
+            want = np.array(getattr(a, n).ndarray)
+            np.testing.assert_array_equal(np.array(getattr(b, n).ndarray), want,
+                                          err_msg=n)
+            np.testing.assert_array_equal(outs[n].array, want, err_msg=n)
+        with pytest.raises(ValueError):
+            b.march_from_host(ins["so1n"], ins["so0n"], 1)
+    finally:
+        b.deliver()
+        for t in list(ins.values()) + list(outs.values()):
+            t.free()
