@@ -18,6 +18,7 @@
 
 #include "../../include/scg.h"
 #include "common.hpp"
+#include "divide.cuh"
 
 #include <cfloat>
 #include <memory>
@@ -43,7 +44,9 @@ struct STArgs
 // (SolutionElement::xctr/dxneg/dxpos/xn/xp, core.hpp:300-360; the CFL
 // half-width and the conservation-element width of
 // update_cfl/march_half_so0, core.hpp:962-980), so the march reads them
-// instead of recomputing them and its results stay bit-identical.
+// instead of recomputing them and its results stay bit-identical.  The four
+// divisors of a half step also get their reciprocals (rcp_tab), from which
+// div_rcp forms each quotient exactly as the division would.
 enum
 {
     G_DXNEG = 0, // x - xneg
@@ -53,6 +56,10 @@ enum
     G_DISP,      // x - xctr
     G_HDX,       // min(x - xneg, xpos - x)
     G_WIDTH,     // xpos - xneg (the width of the element whose top is xi)
+    G_RDXNEG,    // reciprocals of the four divisors
+    G_RDXPOS,
+    G_RHDX,
+    G_RWIDTH,
     G_COUNT
 };
 
@@ -72,8 +79,14 @@ __global__ void k_st_geo(double const * x, int64_t xsize, double * geo)
     geo[G_DMNEG * xsize + xi] = 0.5 * (x0 + xm) - xctr;
     geo[G_DMPOS * xsize + xi] = 0.5 * (x0 + xp) - xctr;
     geo[G_DISP * xsize + xi] = x0 - xctr;
-    geo[G_HDX * xsize + xi] = dn < dp ? dn : dp;
-    geo[G_WIDTH * xsize + xi] = xp - xm;
+    double const hdx = dn < dp ? dn : dp;
+    double const width = xp - xm;
+    geo[G_HDX * xsize + xi] = hdx;
+    geo[G_WIDTH * xsize + xi] = width;
+    geo[G_RDXNEG * xsize + xi] = scg::dev::rcp_tab(dn);
+    geo[G_RDXPOS * xsize + xi] = scg::dev::rcp_tab(dp);
+    geo[G_RHDX * xsize + xi] = scg::dev::rcp_tab(hdx);
+    geo[G_RWIDTH * xsize + xi] = scg::dev::rcp_tab(width);
 }
 
 __device__ __forceinline__ double gq(STArgs const & a, int k, int64_t xi) { return a.geo[k * a.xsize + xi]; }
@@ -81,11 +94,12 @@ __device__ __forceinline__ double gq(STArgs const & a, int k, int64_t xi) { retu
 // The parts of solution element xi that the conservation elements on either
 // side of it use (LinearScalarSelm / InviscidBurgersSelm, xn, xp, tp, so0p):
 // ll = xp + tp (to the element on its right), ur = xn - tp (to the element on
-// its left), the value so0p at the next time level and dxneg, dxpos.
+// its left), the value so0p at the next time level and dxneg, dxpos with
+// their reciprocals.
 template <int KIND>
 struct SelmParts
 {
-    double ll, ur, so0p, dxneg, dxpos;
+    double ll, ur, so0p, dxneg, dxpos, rdxneg, rdxpos;
 
     __device__ SelmParts(STArgs const & a, int64_t xi)
     {
@@ -93,6 +107,8 @@ struct SelmParts
         double const ux = a.so1[xi];
         dxneg = gq(a, G_DXNEG, xi);
         dxpos = gq(a, G_DXPOS, xi);
+        rdxneg = gq(a, G_RDXNEG, xi);
+        rdxpos = gq(a, G_RDXPOS, xi);
         double const disp = gq(a, G_DISP, xi);
         double const xn = dxneg * (u + gq(a, G_DMNEG, xi) * ux);
         double const xp = dxpos * (u + gq(a, G_DMPOS, xi) * ux);
@@ -125,10 +141,11 @@ template <int KIND>
 __device__ __forceinline__ void cfl_at(STArgs const & a, int64_t xi)
 {
     double const hdx = gq(a, G_HDX, xi);
+    double const rhdx = gq(a, G_RHDX, xi);
     if constexpr (KIND == 0)
-        a.cfl[xi] = a.hdt / hdx;
+        a.cfl[xi] = scg::dev::div_rcp(a.hdt, hdx, rhdx);
     else
-        a.cfl[xi] = fabs(a.so0[xi]) * a.hdt / hdx;
+        a.cfl[xi] = scg::dev::div_rcp(fabs(a.so0[xi]) * a.hdt, hdx, rhdx);
 }
 
 template <int ALPHA>
@@ -157,21 +174,24 @@ __global__ void __launch_bounds__(BST) k_st_half(STArgs a, int odd)
     __shared__ double s_ur[BST + 1];
     __shared__ double s_so0p[BST + 1];
     __shared__ double s_dxneg[BST + 1];
+    __shared__ double s_rdxneg[BST + 1];
     int64_t const ic0 = static_cast<int64_t>(blockIdx.x) * BST - (odd ? 1 : 0);
     int64_t const ic = ic0 + threadIdx.x;
     // Solution elements exist for ic <= ncelm (the last one is the
     // lower-right element of conservation element ncelm - 1).
     bool const selm = ic <= a.ncelm;
-    double ll = 0.0, so0pn = 0.0, dxposn = 1.0;
+    double ll = 0.0, so0pn = 0.0, dxposn = 1.0, rdxposn = 1.0;
     if (selm)
     {
         SelmParts<KIND> const sn(a, 2 + 2 * ic + odd);
         ll = sn.ll;
         so0pn = sn.so0p;
         dxposn = sn.dxpos;
+        rdxposn = sn.rdxpos;
         s_ur[threadIdx.x] = sn.ur;
         s_so0p[threadIdx.x] = sn.so0p;
         s_dxneg[threadIdx.x] = sn.dxneg;
+        s_rdxneg[threadIdx.x] = sn.rdxneg;
     }
     if (threadIdx.x == 0)
     {
@@ -182,6 +202,7 @@ __global__ void __launch_bounds__(BST) k_st_half(STArgs a, int odd)
             s_ur[BST] = sh.ur;
             s_so0p[BST] = sh.so0p;
             s_dxneg[BST] = sh.dxneg;
+            s_rdxneg[BST] = sh.rdxneg;
         }
     }
     __syncthreads();
@@ -194,7 +215,7 @@ __global__ void __launch_bounds__(BST) k_st_half(STArgs a, int odd)
     double utp;
     if (STAGE & 1)
     {
-        utp = (ll + s_ur[threadIdx.x + 1]) / gq(a, G_WIDTH, xt);
+        utp = scg::dev::div_rcp(ll + s_ur[threadIdx.x + 1], gq(a, G_WIDTH, xt), gq(a, G_RWIDTH, xt));
         a.so0[xt] = utp;
         if (STAGE & 8)
         {
@@ -221,8 +242,9 @@ __global__ void __launch_bounds__(BST) k_st_half(STArgs a, int odd)
     }
     if (STAGE & 4)
     {
-        double const duxn = (utp - so0pn) / dxposn;
-        double const duxp = (s_so0p[threadIdx.x + 1] - utp) / s_dxneg[threadIdx.x + 1];
+        double const duxn = scg::dev::div_rcp(utp - so0pn, dxposn, rdxposn);
+        double const duxp =
+            scg::dev::div_rcp(s_so0p[threadIdx.x + 1] - utp, s_dxneg[threadIdx.x + 1], s_rdxneg[threadIdx.x + 1]);
         double const g = wgrad<ALPHA>(duxn, duxp);
         a.so1[xt] = g;
         if (STAGE & 8)
@@ -484,6 +506,18 @@ private:
     int graph_alpha = 0;
 };
 
+// One quotient per thread, by div_rcp from the tabulated reciprocal and by
+// the division itself.
+__global__ void k_divide_check(double const * x, double const * d, double * q, double * qdiv, int64_t n)
+{
+    int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        q[i] = scg::dev::div_rcp(x[i], d[i], scg::dev::rcp_tab(d[i]));
+        qdiv[i] = x[i] / d[i];
+    }
+}
+
 } // namespace
 
 struct scg_st
@@ -553,6 +587,28 @@ int scg_st_sync(scg_st * h)
 int scg_st_stream(const scg_st * h, void ** out)
 {
     return scg::guarded([&] { *out = h->c->stream; });
+}
+
+int scg_divide_check(const double * x, const double * d, double * q, double * qdiv, int64_t n)
+{
+    return scg::guarded([&] {
+        if (n < 0 || (n > 0 && (!x || !d || !q || !qdiv)))
+        {
+            throw std::invalid_argument("scg_divide_check: null buffer or negative count");
+        }
+        if (n == 0)
+        {
+            return;
+        }
+        size_t const sz = static_cast<size_t>(n);
+        scg::DevBuf<double> dx(sz), dd(sz), dq(sz), dqd(sz);
+        scg::cuda_check(cudaMemcpy(dx.ptr, x, dx.bytes(), cudaMemcpyHostToDevice), "H2D");
+        scg::cuda_check(cudaMemcpy(dd.ptr, d, dd.bytes(), cudaMemcpyHostToDevice), "H2D");
+        k_divide_check<<<static_cast<unsigned>((n + 255) / 256), 256>>>(dx.ptr, dd.ptr, dq.ptr, dqd.ptr, n);
+        scg::launched(nullptr, "divide_check");
+        scg::cuda_check(cudaMemcpy(q, dq.ptr, dq.bytes(), cudaMemcpyDeviceToHost), "D2H");
+        scg::cuda_check(cudaMemcpy(qdiv, dqd.ptr, dqd.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    });
 }
 
 } // extern "C"
