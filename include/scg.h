@@ -436,8 +436,10 @@ int scg_geometry_round(const double * in, float * out, int64_t n);
 /* Not in the reference: n FP64 quotients x[i] / d[i] on the device, q by
  * the spacetime march's division from a tabulated reciprocal (Markstein's
  * method) and qdiv by the IEEE division, for checking that the two agree bit
- * for bit.  Synchronous; allocates its own device buffers. */
-int scg_divide_check(const double * x, const double * d, double * q, double * qdiv, int64_t n);
+ * for bit; rcp[i] is the multi-dimensional FP64 march's reciprocal of d[i]
+ * (Newton's iteration, within one ulp of 1 / d).  Synchronous; allocates its
+ * own device buffers. */
+int scg_divide_check(const double * x, const double * d, double * q, double * qdiv, double * rcp, int64_t n);
 /* Device FMA throughput in TFLOP/s for SCG_FP64 or SCG_FP32 (a register-only
  * FMA chain over all SMs, iters FMAs-per-accumulator). */
 int scg_fma_peak(int precision, int iters, double * tflops);

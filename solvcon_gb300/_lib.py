@@ -28,7 +28,7 @@ _SIGS = {
     "scg_launch_count": ([], ctypes.c_int64),
     "scg_device_alloc_count": ([], ctypes.c_int64),
     "scg_geometry_round": ([_vp, _vp, ctypes.c_int64], ctypes.c_int),
-    "scg_divide_check": ([_vp, _vp, _vp, _vp, ctypes.c_int64], ctypes.c_int),
+    "scg_divide_check": ([_vp, _vp, _vp, _vp, _vp, ctypes.c_int64], ctypes.c_int),
     "scg_version": ([], ctypes.c_char_p),
     "scg_mesh_create": ([ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                          ctypes.c_int64, _vp], ctypes.c_int),

@@ -456,7 +456,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     constexpr int NEQ = ND + 2;
     R const ga = ldg(a.gamma + row);
     R const ga1 = ga - R(1);
-    R const ri = R(1) / (so0n[0] + Tiny<R>::JAC);
+    R const ri = recip(so0n[0] + Tiny<R>::JAC);
     rinv = ri;
     R momsq = R(0);
 #pragma unroll
@@ -573,7 +573,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
                 delta[d] += s * vob;
             }
         }
-        R const inv = R(1) / (voc * R(ND + 1));
+        R const inv = recip(voc * R(ND + 1));
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
@@ -677,7 +677,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
         {
             pre[k] = pre[k - 1] * dets[k];
         }
-        R inv = R(1) / pre[NFGE - 1];
+        R inv = recip(pre[NFGE - 1]);
 #pragma unroll
         for (int k = NFGE - 1; k > 0; --k)
         {
@@ -780,7 +780,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             R const dd = first ? d1 : d2;
             R const cw = acfl * wacc;
             bool const fire = nn * cw < a.sigma0 * dd;
-            R const c = (fire ? nn : a.sigma0) / (fire ? dd : cw);
+            R const c = (fire ? nn : a.sigma0) * recip(fire ? dd : cw);
             if (fire)
             {
                 fired |= static_cast<uint8_t>(1u << i);

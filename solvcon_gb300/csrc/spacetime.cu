@@ -19,6 +19,7 @@
 #include "../../include/scg.h"
 #include "common.hpp"
 #include "divide.cuh"
+#include "euler_device.cuh"
 
 #include <cfloat>
 #include <memory>
@@ -507,14 +508,16 @@ private:
 };
 
 // One quotient per thread, by div_rcp from the tabulated reciprocal and by
-// the division itself.
-__global__ void k_divide_check(double const * x, double const * d, double * q, double * qdiv, int64_t n)
+// the division itself, and the FP64 march's reciprocal of d.
+__global__ void k_divide_check(double const * x, double const * d, double * q, double * qdiv, double * rcp,
+                               int64_t n)
 {
     int64_t const i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n)
     {
         q[i] = scg::dev::div_rcp(x[i], d[i], scg::dev::rcp_tab(d[i]));
         qdiv[i] = x[i] / d[i];
+        rcp[i] = scg::dev::recip(d[i]);
     }
 }
 
@@ -589,10 +592,10 @@ int scg_st_stream(const scg_st * h, void ** out)
     return scg::guarded([&] { *out = h->c->stream; });
 }
 
-int scg_divide_check(const double * x, const double * d, double * q, double * qdiv, int64_t n)
+int scg_divide_check(const double * x, const double * d, double * q, double * qdiv, double * rcp, int64_t n)
 {
     return scg::guarded([&] {
-        if (n < 0 || (n > 0 && (!x || !d || !q || !qdiv)))
+        if (n < 0 || (n > 0 && (!x || !d || !q || !qdiv || !rcp)))
         {
             throw std::invalid_argument("scg_divide_check: null buffer or negative count");
         }
@@ -601,13 +604,14 @@ int scg_divide_check(const double * x, const double * d, double * q, double * qd
             return;
         }
         size_t const sz = static_cast<size_t>(n);
-        scg::DevBuf<double> dx(sz), dd(sz), dq(sz), dqd(sz);
+        scg::DevBuf<double> dx(sz), dd(sz), dq(sz), dqd(sz), dr(sz);
         scg::cuda_check(cudaMemcpy(dx.ptr, x, dx.bytes(), cudaMemcpyHostToDevice), "H2D");
         scg::cuda_check(cudaMemcpy(dd.ptr, d, dd.bytes(), cudaMemcpyHostToDevice), "H2D");
-        k_divide_check<<<static_cast<unsigned>((n + 255) / 256), 256>>>(dx.ptr, dd.ptr, dq.ptr, dqd.ptr, n);
+        k_divide_check<<<static_cast<unsigned>((n + 255) / 256), 256>>>(dx.ptr, dd.ptr, dq.ptr, dqd.ptr, dr.ptr, n);
         scg::launched(nullptr, "divide_check");
         scg::cuda_check(cudaMemcpy(q, dq.ptr, dq.bytes(), cudaMemcpyDeviceToHost), "D2H");
         scg::cuda_check(cudaMemcpy(qdiv, dqd.ptr, dqd.bytes(), cudaMemcpyDeviceToHost), "D2H");
+        scg::cuda_check(cudaMemcpy(rcp, dr.ptr, dr.bytes(), cudaMemcpyDeviceToHost), "D2H");
     });
 }
 

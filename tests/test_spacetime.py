@@ -202,7 +202,9 @@ def test_division_by_tabulated_reciprocal_is_exact():
     n = x.size
     q = np.empty(n)
     qdiv = np.empty(n)
-    check(lib.scg_divide_check(ptr(x), ptr(d), ptr(q), ptr(qdiv), n))
+    rcp = np.empty(n)
+    check(lib.scg_divide_check(ptr(x), ptr(d), ptr(q), ptr(qdiv), ptr(rcp),
+                               n))
     with np.errstate(all="ignore"):
         want = x / d
     nan = np.isnan(want)
@@ -211,3 +213,33 @@ def test_division_by_tabulated_reciprocal_is_exact():
     assert (qdiv[ok].view(np.uint64) == want[ok].view(np.uint64)).all()
     bad = q[ok].view(np.uint64) != want[ok].view(np.uint64)
     assert not bad.any(), list(zip(x[ok][bad][:5], d[ok][bad][:5]))
+
+
+@pytest.mark.gpu
+def test_march_reciprocal_within_one_ulp():
+    """The FP64 march's reciprocal (Newton's iteration from the FP32
+    hardware seed) is within one ulp of 1 / d for |d| in [2^-1022, 2^1022)
+    of either sign, and the IEEE reciprocal outside it (zeros, subnormals,
+    the largest magnitudes, infinities, NaN)."""
+    from solvcon_gb300._lib import check, lib, ptr
+    x, d = _division_cases()
+    d = np.concatenate([d, [2.0 ** -1021, -2.0 ** -1021, np.nextafter(2.0 ** 1022, 0),
+                            2.0 ** 1022, 2.0 ** -1022, 1e-310, -0.0,
+                            np.finfo(float).max, np.nextafter(1.0, 2.0), 1.0,
+                            np.nextafter(2.0, 0.0)]])
+    x = np.ones_like(d)
+    n = d.size
+    q, qdiv, rcp = np.empty(n), np.empty(n), np.empty(n)
+    check(lib.scg_divide_check(ptr(x), ptr(d), ptr(q), ptr(qdiv), ptr(rcp),
+                               n))
+    with np.errstate(all="ignore"):
+        want = 1.0 / d
+    e = (d.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
+    inside = (e >= 1) & (e <= 2044)
+    gap = np.abs(rcp[inside].view(np.int64) - want[inside].view(np.int64))
+    assert gap.max() <= 1, d[inside][gap > 1][:5]
+    out = ~inside
+    nan = np.isnan(want[out])
+    assert np.isnan(rcp[out][nan]).all()
+    assert (rcp[out][~nan].view(np.uint64) ==
+            want[out][~nan].view(np.uint64)).all()
