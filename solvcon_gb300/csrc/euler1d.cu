@@ -106,6 +106,10 @@ __global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, d
 // the value up at the point, plus the two half fluxes of calc_flux_ll/lr
 // (Euler1DCore.hpp:246-266).  Reciprocals of rho are formed once: for any
 // density above ~1e-50 the reference's denominators rho^k + tiny equal rho^k.
+// The divisions stay IEEE divisions: with the multi-dimensional march's
+// Newton reciprocal (scg::dev::recip) the fine-grained half steps and the
+// fused march, which the reference requires to agree bit for bit, rounded
+// differently (their kernels contracted multiply-adds differently).
 template <typename R>
 struct K1D
 {

@@ -37,6 +37,8 @@
  * every face (a division and about twenty FP64 operations each).
  */
 
+#include "divide.cuh"
+
 #include <cstdint>
 
 namespace scg
@@ -158,47 +160,6 @@ __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double sqr_t(double x) { return sqrt(x); }
 __device__ __forceinline__ float sqr_t(float x) { return sqrtf(x); }
 
-// Reciprocal.  FP64: Newton's iteration r <- r + r (1 - d r) from the FP32
-// hardware approximation of the reciprocal of d's significand (its top 23
-// bits), rescaled by d's exponent; each step squares the relative error, so
-// two take it from ~2^-22 below 2^-86 and r is within one ulp of 1 / d, in
-// four fused multiply-adds (a correctly rounded division takes about twice
-// as many FP64 instructions).  That holds for |d| in [2^-1022, 2^1022);
-// outside it (zero, subnormals, the largest magnitudes, infinities, NaN) the
-// division replaces the result, behind a branch inside one asm statement.
-// The compiler then sees no branch, as it sees none in a division
-// instruction: with the edges taken by branches or selects it could see,
-// kernels inlining this in different code contracted the callers'
-// multiply-adds differently, and batched and single-core marches no longer
-// rounded alike.  A predicated division instead of the branch was issued at
-// every call.  FP32: the division.
-__device__ __forceinline__ double recip(double d)
-{
-    unsigned const hi = static_cast<unsigned>(__double2hiint(d));
-    unsigned const e = (hi >> 20) & 0x7ffu;
-    float const m =
-        __uint_as_float((127u << 23) | ((hi & 0xfffffu) << 3) | (static_cast<unsigned>(__double2loint(d)) >> 29));
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(m));
-    unsigned const yb = __float_as_uint(y);
-    double r = __hiloint2double(static_cast<int>(((yb >> 3) + (896u << 20) - ((e - 1023u) << 20)) | (hi & 0x80000000u)),
-                                static_cast<int>(yb << 29));
-    double t = __fma_rn(-d, r, 1.0);
-    r = __fma_rn(r, t, r);
-    t = __fma_rn(-d, r, 1.0);
-    r = __fma_rn(r, t, r);
-    asm("{\n\t"
-        ".reg .pred p;\n\t"
-        "setp.le.u32 p, %2, 2043;\n\t"
-        "@p bra RCP_DONE;\n\t"
-        "div.rn.f64 %0, 0d3FF0000000000000, %1;\n\t"
-        "RCP_DONE:\n\t"
-        "}"
-        : "+d"(r)
-        : "d"(d), "r"(e - 1u));
-    return r;
-}
-__device__ __forceinline__ float recip(float d) { return 1.0f / d; }
 
 // Compensated (Kahan) accumulator for the FP32 flux sums; plain sum in FP64.
 template <typename R>

@@ -19,7 +19,6 @@
 #include "../../include/scg.h"
 #include "common.hpp"
 #include "divide.cuh"
-#include "euler_device.cuh"
 
 #include <cfloat>
 #include <memory>
