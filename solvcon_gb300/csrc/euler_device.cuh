@@ -161,6 +161,44 @@ __device__ __forceinline__ double sqr_t(double x) { return sqrt(x); }
 __device__ __forceinline__ float sqr_t(float x) { return sqrtf(x); }
 
 
+// The march's reciprocals and quotients.  FP64: recip (Newton) and the
+// division.  FP32 in 2D: the approximate quotient (div.approx.f32, one
+// instruction and within 2 ulp for divisors of magnitude in [2^-126, 2^126];
+// a zero divisor gives a signed infinity, or NaN over zero, as the division
+// does), where a correctly rounded FP32 division is a multi-instruction
+// sequence with a branch and the 2D march divides about a dozen times per
+// cell-substep by densities, determinants, weight sums and CFL numbers, all
+// far inside that range (2M triangles: 0.2352 -> 0.2155 ms per launch).
+// FP32 in 3D: the division (with the approximate quotient the tetrahedron
+// kernel ran 6.45 -> 8.59 ms per launch at the same registers, scheduled
+// differently).
+template <int ND>
+__device__ __forceinline__ double mrecip(double d)
+{
+    return recip(d);
+}
+template <int ND>
+__device__ __forceinline__ float mrecip(float d)
+{
+    if constexpr (ND == 2)
+        return __fdividef(1.0f, d);
+    else
+        return 1.0f / d;
+}
+template <int ND>
+__device__ __forceinline__ double mquot(double x, double y)
+{
+    return x / y;
+}
+template <int ND>
+__device__ __forceinline__ float mquot(float x, float y)
+{
+    if constexpr (ND == 2)
+        return __fdividef(x, y);
+    else
+        return x / y;
+}
+
 // Compensated (Kahan) accumulator for the FP32 flux sums; plain sum in FP64.
 template <typename R>
 struct Acc
@@ -196,7 +234,7 @@ struct Prim
     R ga1;   // gamma - 1
     R vsq;   // |v|^2
 
-    __device__ __forceinline__ Prim(R const * u, R ga) : Prim(u, ga, recip(u[0] + Tiny<R>::JAC)) {}
+    __device__ __forceinline__ Prim(R const * u, R ga) : Prim(u, ga, mrecip<ND>(u[0] + Tiny<R>::JAC)) {}
 
     // With 1/(rho + TINY) already at hand.
     __device__ __forceinline__ Prim(R const * u, R ga, R rinv)

@@ -456,7 +456,7 @@ __device__ __forceinline__ R cfl_cell(MarchArgs<R, G> const & a, int64_t icl, in
     constexpr int NEQ = ND + 2;
     R const ga = ldg(a.gamma + row);
     R const ga1 = ga - R(1);
-    R const ri = recip(so0n[0] + Tiny<R>::JAC);
+    R const ri = mrecip<ND>(so0n[0] + Tiny<R>::JAC);
     rinv = ri;
     R momsq = R(0);
 #pragma unroll
@@ -503,7 +503,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
     using D = Geo<ND, G>;
 
     R const acfl = fabs(cflc);
-    R const sgm0 = sizeof(R) == 8 ? R(0) : a.sigma0 / acfl; // FP32 cap only
+    R const sgm0 = sizeof(R) == 8 ? R(0) : mquot<ND>(a.sigma0, acfl); // FP32 cap only
     R const tau = a.taumin + acfl * a.tauscale;
     R const ofg1 = R(1) / R(NFGE);
 
@@ -573,7 +573,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
                 delta[d] += s * vob;
             }
         }
-        R const inv = recip(voc * R(ND + 1));
+        R const inv = mrecip<ND>(voc * R(ND + 1));
 #pragma unroll
         for (int d = 0; d < ND; ++d)
         {
@@ -691,7 +691,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
 #pragma unroll
         for (int k = 0; k < NFGE; ++k)
         {
-            invs[k] = R(1) / dets[k];
+            invs[k] = mrecip<ND>(dets[k]);
         }
     }
     R C[NFGE][ND][ND];
@@ -799,7 +799,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
         }
         else
         {
-            R const rw = R(1) / wacc;
+            R const rw = mrecip<ND>(wacc);
             R wmax = R(0);
             R wmin = R(0);
 #pragma unroll
@@ -817,7 +817,7 @@ __device__ __forceinline__ void dsoln_cell(MarchArgs<R, G> const & a, int64_t ic
             R const a1 = wmax + Tiny<R>::AZ;
             R const a2 = wmin - Tiny<R>::AZ;
             bool const first = (R(1) - ofg1) * a2 >= -ofg1 * a1;
-            R const sm = (first ? R(1) - ofg1 : -ofg1) / (first ? a1 : a2);
+            R const sm = mquot<ND>(first ? R(1) - ofg1 : -ofg1, first ? a1 : a2);
             R const sig = fmin(sm, sgm0);
             if (sm < sgm0)
             {
