@@ -12,7 +12,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _cores(ndim, precision, seeds, dt_scale=1.0):
+def _cores(ndim, precision, seeds, dt_scale=1.0, mixed=False):
     import solvcon_gb300 as sg
     from solvcon_gb300 import meshgen
     out = []
@@ -20,7 +20,9 @@ def _cores(ndim, precision, seeds, dt_scale=1.0):
         rng = np.random.default_rng(seed)
         if ndim == 2:
             n = int(rng.integers(4, 24))
-            x, t, c = meshgen.tri_square(n, 0.2, seed)
+            gen = meshgen.quad_square if mixed and k % 2 else \
+                meshgen.tri_square
+            x, t, c = gen(n, 0.2, seed)
         else:
             n = int(rng.integers(2, 5))
             gen = meshgen.tet_cube if k % 2 == 0 else meshgen.hex_cube
@@ -67,6 +69,24 @@ def test_batch_equals_individual_marches(ndim, precision):
         a.march(1)
         t.march(1)
         np.testing.assert_array_equal(t.so0n.ndarray, a.so0n.ndarray)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32-geom32"])
+def test_mixed_2d_batch_equals_individual_marches(precision):
+    """Triangle and quadrilateral meshes in one batch: the batch compiles
+    the cell code of both types into one kernel, each core alone a
+    single-type kernel, and the two still round alike."""
+    from solvcon_gb300.batch import EulerBatch
+    seeds = [3, 11, 17, 29]
+    alone = _cores(2, precision, seeds, mixed=True)
+    together = _cores(2, precision, seeds, mixed=True)
+    for _, core in alone:
+        core.march(3)
+    EulerBatch([c for _, c in together], block=128).march(3)
+    for (_, a), (_, t) in zip(alone, together):
+        for name in ("so0n", "so0t", "so1n", "cflo", "cflc"):
+            np.testing.assert_array_equal(getattr(t, name).ndarray,
+                                          getattr(a, name).ndarray, name)
 
 
 def test_autotune_candidates_agree():
