@@ -145,7 +145,10 @@ int scg_mesh_from_plot3d(const char * data, int64_t nbyte, scg_mesh ** out);
 #define SCG_FP64 0        /* the reference's FP64 arithmetic */
 /* The FP32 form of the EulerCore: FP32 state and flux arithmetic with
  * compensated face sums, mesh geometry kept in FP64 tables, FP64 totals and
- * CFL reduction. */
+ * CFL reduction.  The march rounds the FP64 geometry to FP32 where it uses
+ * it; a mesh whose geometry (at this time increment) reaches 2^128 in
+ * magnitude, or holds infinities or NaN, is refused with SCG_EINVAL when the
+ * core is created or one of its CE geometry arrays is set. */
 #define SCG_FP32_GEOM64 1
 /* A faster EulerCore variant beside it: the same FP32 march with its
  * geometry (computed in FP64) stored in FP32, ~35% less traffic per cell. */
@@ -430,8 +433,9 @@ int scg_st_stream(const scg_st * solver, void ** out);
 
 /* Not in the reference: round n FP64 values to FP32 on the device exactly as
  * the FP32 march rounds its FP64 geometry tables where it uses them
- * (round to nearest even, formed on the integer pipe), for checking that
- * rounding.  Synchronous; allocates its own device buffers. */
+ * (round to nearest even, formed on the integer pipe; values below FP32's
+ * normal range give a signed zero, and values of magnitude 2^128 and beyond,
+ * which a core refuses, are not defined here), for checking that rounding.  Synchronous; allocates its own device buffers. */
 int scg_geometry_round(const double * in, float * out, int64_t n);
 /* Not in the reference: n FP64 quotients x[i] / d[i] on the device, q by
  * the spacetime march's division from a tabulated reciprocal (Markstein's

@@ -857,6 +857,10 @@ public:
         // Geometry: prepare_ce, then the compact march tables.
         d_fgeo.alloc(static_cast<size_t>(std::max(nslot, 1)) * KF * std::max<int64_t>(ncell, 1));
         d_cgeo.alloc(static_cast<size_t>(Dim<ND>::KC) * std::max<int64_t>(ncell, 1));
+        // Slots past a cell's own faces are never written; zero them so the
+        // whole tables hold defined values (the FP32 form checks them all).
+        cuda_check(cudaMemsetAsync(d_fgeo.ptr, 0, d_fgeo.bytes(), stream), "memset");
+        cuda_check(cudaMemsetAsync(d_cgeo.ptr, 0, d_cgeo.bytes(), stream), "memset");
         d_nbr.alloc(static_cast<size_t>(std::max(nslot, 1)) * std::max<int64_t>(ncell, 1));
         d_ctype.alloc(std::max<int64_t>(ncell, 1));
         prepare_ce(true);
@@ -1049,6 +1053,36 @@ public:
                                                                 0.5 * time_increment, std::max(nslot, 1),
                                                                 d_fgeo.ptr, d_cgeo.ptr, d_nbr.ptr, d_ctype.ptr);
         launched(stream, "compact");
+        if constexpr (sizeof(R) == 4 && sizeof(G) == 8)
+        {
+            check_geometry_range();
+        }
+    }
+
+    // The FP32 march rounds its FP64 geometry without range selects
+    // (scg::dev::geo_r): refuse tables holding values it does not take.
+    void check_geometry_range()
+    {
+        DevBuf<unsigned long long> bad(1);
+        cuda_check(cudaMemsetAsync(bad.ptr, 0, sizeof(unsigned long long), stream), "memset");
+        for (auto const * t : {&d_fgeo, &d_cgeo})
+        {
+            int64_t const n = static_cast<int64_t>(t->bytes() / sizeof(G));
+            int64_t const blocks = std::min<int64_t>((n + BLOCK - 1) / BLOCK, 4096);
+            k_geo_range<<<static_cast<unsigned>(std::max<int64_t>(blocks, 1)), BLOCK, 0, stream>>>(
+                reinterpret_cast<double const *>(t->ptr), n, bad.ptr);
+            launched(stream, "geo_range");
+        }
+        unsigned long long cnt = 0;
+        cuda_check(cudaMemcpyAsync(&cnt, bad.ptr, sizeof(cnt), cudaMemcpyDeviceToHost, stream), "D2H");
+        sync();
+        if (cnt)
+        {
+            throw std::invalid_argument("EulerCore: precision fp32 keeps FP64 geometry and uses it in FP32; " +
+                                        std::to_string(cnt) +
+                                        " geometry values of this mesh lie beyond FP32's range (magnitude 2^128 "
+                                        "or more, infinite or NaN): use precision fp64, or rescale the mesh");
+        }
     }
 
     // ---- boundary conditions ---------------------------------------------

@@ -122,16 +122,28 @@ struct Tiny<float>
 // float conversion instruction issues on the FP64 pipe (16 cycles per warp on
 // GB300, measured), and the FP32 march converts ~60 geometry values per
 // cell-substep, which made that pipe the FP32 march's bottleneck.  In the
-// FP32 normal range the result is IEEE round-to-nearest-even: the word formed
-// by funnel-shifting the sign-less high word left by 3 (taking the low word's
-// top 3 bits) holds the exponent and the top 23 mantissa bits in place, and
-// subtracting (1023 - 127) << 23 modulo 2^32 rebiases the exponent (its
-// high bits shifted out cancel); the 29 dropped bits then round it:
-// (dropped + lsb + 2^28 - 1) >> 29 is 1 exactly when they exceed half, or
-// equal half with an odd lsb.  Values below the FP32 normal range become a
-// signed zero; values beyond it, infinities and NaNs become NaN (no mesh
-// produces them, and a broken table then shows).  Branch-free, so nothing
-// falls back to the conversion instruction.
+// FP32 normal range the result is IEEE round-to-nearest-even: adding
+// 2^28 - 1 plus the kept part's lowest bit to the 64-bit pattern carries
+// into bit 29 exactly when the 29 bits to be dropped exceed half, or equal
+// half with an odd lowest kept bit; the funnel shift then takes bits 29..60,
+// the exponent and the top 23 mantissa bits in place, and subtracting
+// (1023 - 127) << 23 modulo 2^32 rebiases the exponent (its high bits
+// shifted out cancel).  Values below the FP32 normal range (round-off
+// residue in the tables) become a signed zero, by one compare and select.
+// Larger ones are not taken here: a core of the FP32 form checks its
+// geometry tables when it builds them (k_geo_range) and refuses values at
+// 2^128 and beyond, infinities and NaNs, so the rounding needs no second
+// range select (9 integer instructions per value instead of 15, for ~47
+// values per cell-substep in 2D).  Branch-free, so nothing falls back to the
+// conversion instruction.
+// The geometry values geo_r takes: magnitudes below 2^128 (biased exponent
+// up to 1150).
+__device__ __forceinline__ bool geo_r_takes(double v)
+{
+    unsigned const e = (static_cast<unsigned>(__double2hiint(v)) >> 20) & 0x7FFu;
+    return e <= 1150u;
+}
+
 template <typename R, typename G>
 __device__ __forceinline__ R geo_r(G v)
 {
@@ -139,13 +151,10 @@ __device__ __forceinline__ R geo_r(G v)
     {
         unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
         unsigned const hi = static_cast<unsigned>(b >> 32);
-        unsigned const lo = static_cast<unsigned>(b);
-        unsigned const ahi = hi & 0x7FFFFFFFu;
-        unsigned const e = ahi >> 20;
-        unsigned r = __funnelshift_l(lo, ahi, 3) - 0xC0000000u;
-        r += ((lo & 0x1FFFFFFFu) + (r & 1u) + 0x0FFFFFFFu) >> 29;
-        r = (e - 897u < 254u) ? r : (e > 1150u ? 0x7FC00000u : 0u);
-        return __uint_as_float(r | (hi & 0x80000000u));
+        unsigned long long const t = b + 0x0FFFFFFFull + ((b >> 29) & 1ull);
+        unsigned const r =
+            __funnelshift_l(static_cast<unsigned>(t), static_cast<unsigned>(t >> 32), 3) - 0xC0000000u;
+        return __uint_as_float(((hi & 0x7FF00000u) >= (897u << 20) ? r : 0u) | (hi & 0x80000000u));
     }
     else
     {

@@ -40,6 +40,22 @@ struct MeshView
 // cell icl, its face count and faces, each face's two cells (one of them icl)
 // and its node count and nodes.  Reads only inside the tables; the first bad
 // cell lands in *bad (atomicMin).
+// Count the values of an FP64 geometry table that the FP32 march's rounding
+// (geo_r) does not take.
+__global__ void k_geo_range(double const * g, int64_t n, unsigned long long * bad)
+{
+    unsigned long long cnt = 0;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        cnt += geo_r_takes(g[i]) ? 0ull : 1ull;
+    }
+    if (cnt)
+    {
+        atomicAdd(bad, cnt);
+    }
+}
+
 __global__ void k_validate_mesh(MeshView m, int64_t nface, int64_t nnode, unsigned long long * bad)
 {
     int64_t const icl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;

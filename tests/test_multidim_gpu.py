@@ -617,9 +617,10 @@ def test_geometry_rounding_is_round_to_nearest_even():
     instructions; on the device that rounding equals IEEE
     round-to-nearest-even (numpy's float64 -> float32) bit for bit over the
     FP32 normal range: random values, exact ties, near-ties, mantissa
-    carries into the exponent.  Zero keeps its sign, values below the normal
-    range become a signed zero, and values beyond it, infinities and NaNs
-    become NaN."""
+    carries into the exponent (up to infinity from the top binade).  Values
+    below the normal range become a signed zero.  Larger ones are not taken:
+    a core of the FP32 form refuses a mesh whose geometry holds them (tested
+    below)."""
     from solvcon_gb300._lib import check, lib, ptr
     rng = np.random.default_rng(5)
     n = 1 << 20
@@ -633,22 +634,37 @@ def test_geometry_rounding_is_round_to_nearest_even():
         bits[sl] = (bits[sl] & ~low) | np.uint64(pat)
     bits[200000:250000] |= np.uint64((1 << 52) - 1)
     x = bits.view(np.float64).copy()
-    x[:8] = [0.0, -0.0, 1e-40, -3e-39, 1e39, np.inf, -np.inf, np.nan]
+    x[:10] = [0.0, -0.0, 1e-40, -3e-39, 1e39, np.inf, -np.inf, np.nan,
+              5e-324, -1e-310]
     got = np.empty(n, dtype=np.float32)
     check(lib.scg_geometry_round(ptr(x), ptr(got), n))
     with np.errstate(over="ignore"):
         want = x.astype(np.float32)
-    e = (bits >> np.uint64(52)) & np.uint64(0x7FF)
-    e[:8] = [0, 0, 874, 872, 1200, 2047, 2047, 2047]
+    e = (x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)
     normal = (e >= 897) & (e <= 1150)
     g, w = got.view(np.uint32), want.view(np.uint32)
     same = g[normal] == w[normal]
     assert same.all(), x[normal][~same][:5]
     tiny = e < 897
+    assert tiny.sum() >= 6
     assert (got[tiny] == 0).all()
     assert (np.signbit(got[tiny]) == np.signbit(x[tiny])).all()
-    assert np.isnan(got[e > 1150]).all()
 
+
+
+def test_fp32_form_refuses_geometry_outside_fp32_range():
+    """The FP32 form keeps FP64 geometry and rounds it where it is used,
+    without an overflow check; a mesh whose geometry goes beyond FP32's
+    range (a unit square scaled by 1e25: areas of 1e50) is refused when the
+    core is built, and marches in FP64 as before."""
+    import solvcon_gb300 as sg
+    from solvcon_gb300 import meshgen
+    x, t, c = meshgen.tri_square(6, 0.2, seed=1)
+    mesh = meshgen.build_mesh(2, x * 1e25, t, c)
+    with pytest.raises(ValueError, match="beyond FP32's range"):
+        sg.EulerCore(mesh, 1e20, precision="fp32")
+    ec = sg.EulerCore(mesh, 1e20, precision="fp64")
+    assert ec.ncell == mesh.ncell
 
 @pytest.mark.parametrize("precision", ["fp32", "fp32-geom32"])
 def test_fp32_state_keeps_its_rounding_residual(precision):
