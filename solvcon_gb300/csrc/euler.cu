@@ -1555,7 +1555,12 @@ public:
     // FP32: the registered host blocks receive the state after the march.
     void gather_delivery(bool delivers)
     {
-        if (sizeof(R) == 8 || !delivers)
+        if constexpr (sizeof(R) == 8)
+        {
+            (void)delivers;
+            return;
+        }
+        if (!delivers)
         {
             return;
         }
