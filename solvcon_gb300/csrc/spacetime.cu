@@ -60,6 +60,7 @@ enum
     G_RDXPOS,
     G_RHDX,
     G_RWIDTH,
+    G_CFLLIN,    // the linear solver's CFL number hdt / hdx (set with dt)
     G_COUNT
 };
 
@@ -137,15 +138,25 @@ struct SelmParts
     }
 };
 
+// The linear solver's CFL number at every point, hdt / hdx: it depends on
+// the grid and the time increment alone, so it is formed when either is set
+// (the same quotient the half step would form) and the half steps copy it.
+__global__ void k_st_cfl_tab(double * geo, int64_t xsize, double hdt)
+{
+    int64_t const xi = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (xi < xsize)
+    {
+        geo[G_CFLLIN * xsize + xi] = scg::dev::div_rcp(hdt, geo[G_HDX * xsize + xi], geo[G_RHDX * xsize + xi]);
+    }
+}
+
 template <int KIND>
 __device__ __forceinline__ void cfl_at(STArgs const & a, int64_t xi)
 {
-    double const hdx = gq(a, G_HDX, xi);
-    double const rhdx = gq(a, G_RHDX, xi);
     if constexpr (KIND == 0)
-        a.cfl[xi] = scg::dev::div_rcp(a.hdt, hdx, rhdx);
+        a.cfl[xi] = gq(a, G_CFLLIN, xi);
     else
-        a.cfl[xi] = scg::dev::div_rcp(fabs(a.so0[xi]) * a.hdt, hdx, rhdx);
+        a.cfl[xi] = scg::dev::div_rcp(fabs(a.so0[xi]) * a.hdt, gq(a, G_HDX, xi), gq(a, G_RHDX, xi));
 }
 
 template <int ALPHA>
@@ -329,6 +340,15 @@ public:
             cudaGraphExecDestroy(graph_exec);
             graph_exec = nullptr;
         }
+        make_cfl_tab();
+    }
+
+    void make_cfl_tab()
+    {
+        k_st_cfl_tab<<<static_cast<unsigned>((xsize + 255) / 256), 256, 0, stream>>>(geo.ptr, xsize,
+                                                                                     0.5 * time_increment);
+        scg::launched(stream, "spacetime_cfl_tab");
+        sync();
     }
 
     STArgs args()
@@ -343,7 +363,7 @@ public:
         scg::cuda_check(cudaMemsetAsync(geo.ptr, 0, geo.bytes(), stream), "memset");
         k_st_geo<<<static_cast<unsigned>((xsize + 255) / 256), 256, 0, stream>>>(x.ptr, xsize, geo.ptr);
         scg::launched(stream, "spacetime_geo");
-        sync();
+        make_cfl_tab();
     }
 
     double * field(int which)
