@@ -20,6 +20,7 @@
 
 #include "../../include/scg.h"
 #include "common.hpp"
+#include "divide.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -106,10 +107,9 @@ __global__ void k_inv_spacing(double const * coord, int64_t n, double * invdx, d
 // the value up at the point, plus the two half fluxes of calc_flux_ll/lr
 // (Euler1DCore.hpp:246-266).  Reciprocals of rho are formed once: for any
 // density above ~1e-50 the reference's denominators rho^k + tiny equal rho^k.
-// The divisions stay IEEE divisions: with the multi-dimensional march's
-// Newton reciprocal (scg::dev::recip) the fine-grained half steps and the
-// fused march, which the reference requires to agree bit for bit, rounded
-// differently (their kernels contracted multiply-adds differently).
+// Its divisions (this one, update_cfl's and the W-alpha weights') multiply
+// by scg::dev::recip, a Newton reciprocal within one ulp that takes about
+// half the FP64 instructions of a division.
 template <typename R>
 struct K1D
 {
@@ -129,7 +129,7 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
         u[i] = a.so0[ic * 3 + i];
         ux[i] = a.so1[ic * 3 + i];
     }
-    R const r = R(1) / (u[0] + Tiny1D<R>::V);
+    R const r = scg::dev::recip(u[0] + Tiny1D<R>::V);
     k.r = r;
     R const r2 = r * r;
     R const m2r2 = u[1] * u[1] * r2; // u1^2 / u0^2
@@ -180,7 +180,7 @@ __device__ __forceinline__ void derive(E1DArgs<R> const & a, int64_t ic, K1D<R> 
 template <typename R>
 __device__ __forceinline__ R rho_recip(E1DArgs<R> const & a, int64_t it)
 {
-    return R(1) / (a.so0[it * 3 + 0] + Tiny1D<R>::V);
+    return scg::dev::recip(a.so0[it * 3 + 0] + Tiny1D<R>::V);
 }
 
 __device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
@@ -200,31 +200,42 @@ __device__ __forceinline__ void cfl_at(E1DArgs<R> const & a, int64_t it, double 
     R const wspd = sqrt_r(ga * pr * r) + fabs(m) * r;
     double const dxpos = a.coord[it + 1] - a.coord[it];
     double const dxneg = a.coord[it] - a.coord[it - 1];
-    a.cfl[it] = R(hdt) * wspd / R(dxpos < dxneg ? dxpos : dxneg);
+    a.cfl[it] = R(hdt) * wspd * scg::dev::recip(R(dxpos < dxneg ? dxpos : dxneg));
 }
 
 // The W-alpha gradient (march_half_so1_alpha, Euler1DCore.hpp:284-320).
-template <int ALPHA, typename R>
-__device__ __forceinline__ R wgrad(R duxn, R duxp)
+template <typename R>
+__device__ __forceinline__ R wgrad(int alpha, R duxn, R duxp)
 {
     R fan = fabs(duxn);
     R fap = fabs(duxp);
-    if constexpr (ALPHA == 2)
+    if (alpha == 2)
     {
         fan *= fan;
         fap *= fap;
     }
-    return (fap * duxn + fan * duxp) / (fap + fan + Tiny1D<R>::V);
+    return (fap * duxn + fan * duxp) * scg::dev::recip(fap + fan + Tiny1D<R>::V);
 }
 
-// Fused half step: so0, cfl and (when ALPHA > 0) so1 at one parity; with
-// BND also the copy-out boundary treatment (Euler1DCore.cpp:132-172).
-// Output j is point start + 2j + 1 for j < nout; kernels are at start + 2j for
-// j <= nout.
-template <int ALPHA, bool DO_SO0, bool DO_CFL, bool BND, typename R>
-__global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64_t nout)
+// What a half step does (k_half's mask): so0, cfl, the copy-out boundary
+// treatment, and so1 with the W-alpha weights for alpha = (mask >> 8) > 0.
+constexpr unsigned H_SO0 = 1u, H_CFL = 2u, H_BND = 4u;
+constexpr unsigned h_alpha(int alpha) { return static_cast<unsigned>(alpha) << 8; }
+
+// Fused half step: so0, cfl and (alpha > 0) so1 at one parity, with the
+// copy-out boundary treatment (Euler1DCore.cpp:132-172), each as the mask
+// asks.  Output j is point start + 2j + 1 for j < nout; kernels are at
+// start + 2j for j <= nout.  The mask is a launch argument, not a template
+// parameter: the fine-grained operations (march_half_so0, then
+// march_half_so1_alpha on the so0 it stored) and the fused march then run
+// the same compiled code and round alike, which the reference requires of
+// its two marches; compiled apart, the kernels contracted their
+// multiply-adds differently once the divisions became Newton reciprocals.
+template <typename R>
+__global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64_t nout, unsigned mask)
 {
     {
+        int const alpha = static_cast<int>(mask >> 8);
         __shared__ R s_lr[B1D + 1][3];
         __shared__ R s_up[B1D + 1][3];
         __shared__ R s_idxr[B1D + 1]; // 1 / (x - xneg) of each kernel
@@ -262,7 +273,7 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
         {
             int64_t const ic = start + 2 * j;
             R v[3];
-            if (DO_SO0)
+            if (mask & H_SO0)
             {
                 R const idx = R(a.invd2[ic]);
                 for (int i = 0; i < 3; ++i)
@@ -278,11 +289,11 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                     v[i] = a.so0[(ic + 1) * 3 + i];
                 }
             }
-            if (DO_CFL)
+            if (mask & H_CFL)
             {
                 cfl_at(a, ic, a.hdt, k.r);
             }
-            if constexpr (ALPHA > 0)
+            if (alpha > 0)
             {
                 R const idn = R(a.invdx[ic]);
                 R const idp = s_idxr[threadIdx.x + 1];
@@ -290,11 +301,11 @@ __global__ void __launch_bounds__(B1D) k_half(E1DArgs<R> a, int64_t start, int64
                 {
                     R const duxn = (v[i] - k.up[i]) * idn;
                     R const duxp = (s_up[threadIdx.x + 1][i] - v[i]) * idp;
-                    a.so1[(ic + 1) * 3 + i] = wgrad<ALPHA>(duxn, duxp);
+                    a.so1[(ic + 1) * 3 + i] = wgrad(alpha, duxn, duxp);
                 }
             }
         }
-        if (BND && blockIdx.x == 0 && threadIdx.x == 0)
+        if ((mask & H_BND) && blockIdx.x == 0 && threadIdx.x == 0)
         {
             int64_t const l = 1, r = a.n - 2;
             for (int i = 0; i < 3; ++i)
@@ -480,13 +491,12 @@ public:
         nout = stop > start ? (stop - start + 1) / 2 : 0;
     }
 
-    template <int ALPHA, bool SO0, bool CFL, bool BND>
-    void half(bool odd)
+    void half(unsigned mask, bool odd)
     {
         int64_t start, nout;
         range(odd, start, nout);
         unsigned const grid = static_cast<unsigned>((nout + B1D) / B1D);
-        k_half<ALPHA, SO0, CFL, BND, R><<<grid, B1D, 0, stream>>>(args(), start, nout);
+        k_half<R><<<grid, B1D, 0, stream>>>(args(), start, nout, mask);
         scg::launched(stream, "e1d_half");
     }
 
@@ -506,13 +516,10 @@ public:
             break;
         }
         case 1: // march_half_so0
-            half<0, true, false, false>(odd != 0);
+            half(H_SO0, odd != 0);
             break;
         case 2: // march_half_so1_alpha
-            if (alpha == 1)
-                half<1, false, false, false>(odd != 0);
-            else
-                half<2, false, false, false>(odd != 0);
+            half(h_alpha(alpha == 1 ? 1 : 2), odd != 0);
             break;
         case 3: // treat_boundary_so0
         case 4: // treat_boundary_so1
@@ -531,16 +538,10 @@ public:
             break;
         }
         case 6: // march_half1_alpha: so0, cfl, so1 at the even kernels
-            if (alpha == 1)
-                half<1, true, true, false>(false);
-            else
-                half<2, true, true, false>(false);
+            half(H_SO0 | H_CFL | h_alpha(alpha == 1 ? 1 : 2), false);
             break;
         case 7: // march_half2_alpha
-            if (alpha == 1)
-                half<1, true, true, false>(true);
-            else
-                half<2, true, true, false>(true);
+            half(H_SO0 | H_CFL | h_alpha(alpha == 1 ? 1 : 2), true);
             break;
         default:
             throw std::invalid_argument("Euler1DCore: unknown operation " + std::to_string(which));
@@ -552,16 +553,8 @@ public:
     // boundary treatment fused, then half 2.
     void step(int alpha)
     {
-        if (alpha == 1)
-        {
-            half<1, true, true, true>(false);
-            half<1, true, true, false>(true);
-        }
-        else
-        {
-            half<2, true, true, true>(false);
-            half<2, true, true, false>(true);
-        }
+        half(H_SO0 | H_CFL | H_BND | h_alpha(alpha), false);
+        half(H_SO0 | H_CFL | h_alpha(alpha), true);
     }
 
     // march_alpha(steps): chunks of GRAPH_STEPS steps replay one captured
